@@ -1,0 +1,334 @@
+"""TimeEvolutionProblem / TimeEvolutionResult with the reference's interface.
+
+Mirrors pyjjasim time_evolution.py so that code written against the reference runs
+unchanged here, with the per-step core executed on the GPU:
+
+* ``TimeEvolutionProblem`` (time_evolution.py:20-409): same constructor arguments,
+  problem-count inference (:110-116), broadcasting of sources to (N, W, Nt) views or
+  kept callables (:119-130), store masks (:132-140, 384-399), stencils (:401-408),
+  initial conditions (:144-149, 327-332) and per-step accessors ``_f/_Is/_Vs/_T``
+  (:342-356).
+* ``time_evolution`` (time_evolution.py:422-458): widens the store masks so the
+  voltage stencil has its previous steps, calls the core, derives V, strips helper
+  steps. The core is the GPU backend (``pyjjasim_gb300.backend.time_evolution_core``).
+* ``TimeEvolutionResult`` (time_evolution.py:597-1067): theta / current / voltage /
+  vortex configuration accessors with the same shapes and errors.
+"""
+import numpy as np
+
+__all__ = ["DefaultCPR", "TimeEvolutionProblem", "TimeEvolutionResult", "time_evolution",
+           "ThetaNotStored", "CurrentNotStored", "VoltageNotStored", "DataAtTimepointNotStored"]
+
+
+class DefaultCPR:
+    """Current-phase relation Ic*sin(theta) (static_problem.py:77-85)."""
+
+    def eval(self, Ic, theta):
+        return Ic * np.sin(theta)
+
+    def d_eval(self, Ic, theta):
+        return Ic * np.cos(theta)
+
+    def i_eval(self, Ic, theta):
+        return Ic * (1.0 - np.cos(theta))
+
+
+def stencil(width):
+    """Backward stencils (first derivative, second derivative) of width 3, 4 or 5."""
+    if width == 3:
+        return (1.0, -1.0, 0.0), (1.0, -2.0, 1.0)
+    if width == 4:
+        return (1.5, -2.0, 0.5, 0.0), (2.0, -5.0, 4.0, -1.0)
+    if width == 5:
+        return (11.0 / 6, -3.0, 1.5, -1.0 / 3, 0.0), (35.0 / 12, -26.0 / 3, 9.5, -14.0 / 3, 11.0 / 12)
+    raise ValueError(f"stencil width must be 3, 4 or 5 (equals {width})")
+
+
+class TimeEvolutionProblem:
+    """W time-evolution problems on one Josephson circuit (see time_evolution.py:20-92).
+
+    Arrays are broadcast to (Nf|Nj, W, Nt) read-only views; callables f(i) -> (N, W)
+    are evaluated per step. ``compute()`` runs the GPU backend.
+    """
+
+    def __init__(self, circuit, time_step=0.05, time_step_count=1000, current_phase_relation=None,
+                 external_flux=0.0, current_sources=0.0, voltage_sources=0.0, temperature=0.0,
+                 store_time_steps=None, store_theta=True, store_voltage=True, store_current=True,
+                 config_at_minus_1=None, config_at_minus_2=None, config_at_minus_3=None,
+                 config_at_minus_4=None, stencil_width=3):
+        self.circuit = circuit
+        self.time_step = time_step
+        self.time_step_count = time_step_count
+        self.current_phase_relation = DefaultCPR() if current_phase_relation is None else current_phase_relation
+
+        def count(x):
+            s = np.array(x(0) if callable(x) else x).shape
+            return s[1] if len(s) > 1 else 1
+
+        self.problem_count = max(count(external_flux), count(current_sources), count(voltage_sources),
+                                 count(temperature))
+        Nj, Nf, W, Nt = circuit._Nj(), circuit._Nf(), self.problem_count, time_step_count
+
+        def prep(x, N):
+            return x if callable(x) else np.broadcast_to(np.array(x), (N, W, Nt))
+
+        self._f_is_timedep = self._is_timedep(external_flux)
+        self.external_flux = prep(external_flux, Nf)
+        self._Is_is_timedep = self._is_timedep(current_sources)
+        self.current_sources = prep(current_sources, Nj)
+        self._Vs_is_timedep = self._is_timedep(voltage_sources)
+        self.voltage_sources = prep(voltage_sources, Nj)
+        self._T_is_timedep = self._is_timedep(temperature)
+        self.temperature = prep(temperature, Nj)
+
+        self.store_time_steps = np.ones(Nt, dtype=bool)
+        self.store_time_steps = self._to_time_point_mask(store_time_steps)
+        self.store_theta, self.store_voltage, self.store_current = store_theta, store_voltage, store_current
+        if not (store_theta or store_voltage or store_current):
+            raise ValueError("No output is stored")
+        if np.sum(self.store_time_steps) == 0:
+            raise ValueError("No output is stored")
+        self.stencil_width = stencil_width
+        self.stencil = stencil(stencil_width)
+        zeros = np.zeros((Nj, W), dtype=np.double)
+        self.config_at_minus_1 = self._get_config(config_at_minus_1, zeros, (Nj, W))
+        self.config_at_minus_2 = self._get_config(config_at_minus_2, self.config_at_minus_1, (Nj, W))
+        if stencil_width >= 4:
+            self.config_at_minus_3 = self._get_config(config_at_minus_3, self.config_at_minus_2, (Nj, W))
+        if stencil_width >= 5:
+            self.config_at_minus_4 = self._get_config(config_at_minus_4, self.config_at_minus_3, (Nj, W))
+
+    # --- public getters (time_evolution.py:172-301) -----------------------------------------
+    def get_problem_count(self):
+        return self.problem_count
+
+    def get_circuit(self):
+        return self.circuit
+
+    def get_time_step(self):
+        return self.time_step
+
+    def get_time_step_count(self):
+        return self.time_step_count
+
+    def get_current_phase_relation(self):
+        return self.current_phase_relation
+
+    def get_external_flux(self):
+        return self.external_flux
+
+    def get_current_sources(self):
+        return self.current_sources
+
+    def get_voltage_sources(self):
+        return self.voltage_sources
+
+    def get_temperature(self):
+        return self.temperature
+
+    def get_store_time_steps(self):
+        return self.store_time_steps
+
+    def get_store_theta(self):
+        return self.store_theta
+
+    def get_store_voltage(self):
+        return self.store_voltage
+
+    def get_store_current(self):
+        return self.store_current
+
+    def get_time(self):
+        return np.arange(self._Nt(), dtype=np.double) * self._dt()
+
+    def compute(self, backend="gb300", **options):
+        """Run the time evolution and return a TimeEvolutionResult.
+
+        ``backend="gb300"`` (the only backend) executes the per-step core on the GPU.
+        ``options`` are forwarded to it (``noise="philox"|"numpy"``, ``seed``,
+        ``precision``, ``device``).
+        """
+        if backend != "gb300":
+            raise ValueError(f"unknown backend {backend!r}; this package provides 'gb300' only")
+        return time_evolution(self, **options)
+
+    # --- internal accessors (time_evolution.py:315-408) -------------------------------------
+    def _Nt(self):
+        return self.time_step_count
+
+    def _Nt_s(self):
+        return int(np.sum(self.store_time_steps))
+
+    def _dt(self):
+        return self.time_step
+
+    @staticmethod
+    def _get_config(cur, prev, shape):
+        cur = prev.copy() if cur is None else cur
+        if hasattr(cur, "get_theta"):
+            cur = cur.get_theta()
+        return np.asarray(cur, dtype=np.double).reshape(shape)
+
+    @staticmethod
+    def _is_timedep(x):
+        if callable(x):
+            return True
+        s = np.array(x).shape
+        return len(s) > 0 and s[-1] > 1
+
+    def _step_value(self, x, N, i):
+        if callable(x):
+            return np.broadcast_to(x(i), (N, self.problem_count))
+        return x[:, :, i]
+
+    def _f(self, i):
+        return self._step_value(self.external_flux, self.circuit._Nf(), i)
+
+    def _Is(self, i):
+        return self._step_value(self.current_sources, self.circuit._Nj(), i)
+
+    def _Vs(self, i):
+        return self._step_value(self.voltage_sources, self.circuit._Nj(), i)
+
+    def _T(self, i):
+        return self._step_value(self.temperature, self.circuit._Nj(), i)
+
+    def _cp(self, theta):
+        return self.current_phase_relation.eval(self.circuit._Ic()[:, None], theta)
+
+    def _to_time_point_mask(self, time_points):
+        if time_points is None:
+            time_points = self.store_time_steps
+        time_points = np.array(time_points)
+        if time_points.dtype != bool:
+            try:
+                m = np.zeros(self._Nt(), dtype=bool)
+                m[time_points] = True
+                time_points = m
+            except Exception:
+                raise ValueError("Invalid store_time_steps; must be None, mask, slice or index array")
+        return time_points
+
+
+def _stencil_derivative(x, index, s1, dt):
+    out = s1[0] * x[:, :, index]
+    for k in range(1, len(s1) - 1):
+        out = out + s1[k] * x[:, :, index - k]
+    return out / dt
+
+
+def time_evolution(problem, **options):
+    """Driver around the GPU core: masks, core call, voltage (time_evolution.py:422-458)."""
+    from .backend import time_evolution_core
+    Nt = problem._Nt()
+    store = np.asarray(problem.store_time_steps, bool)
+    th_mask = store.copy() if (problem.store_theta or problem.store_voltage) else np.zeros(Nt, bool)
+    I_mask = store.copy() if (problem.store_current or problem.store_voltage) else np.zeros(Nt, bool)
+    Vth_mask, VI_mask = th_mask.copy(), I_mask.copy()
+    t_ids = np.flatnonzero(store)
+    c = problem.get_circuit()
+    offset = problem.stencil_width - 1
+    if problem.store_voltage and len(t_ids) > 0:
+        ids = (t_ids[:, None] - np.arange(offset)).ravel()
+        ids = ids[(ids >= 0) & (ids < Nt)]
+        Vth_mask[ids] = True
+        if c._has_inductance():
+            VI_mask[ids] = True
+    th_out, I_out = time_evolution_core(problem, Vth_mask, VI_mask, **options)
+    V = None
+    if problem.store_voltage:
+        ts = np.flatnonzero(store[Vth_mask])
+        V = _stencil_derivative(th_out, ts + offset, problem.stencil[0], problem._dt())
+        if c._has_inductance():
+            VI = _stencil_derivative(I_out, ts + offset, problem.stencil[0], problem._dt())
+            V = V + (c.get_inductance() @ VI.reshape((c._Nj(), -1))).reshape(V.shape)
+        th_out = np.delete(th_out, np.flatnonzero((Vth_mask & ~th_mask)[Vth_mask]) + offset, axis=2)
+        I_out = np.delete(I_out, np.flatnonzero((VI_mask & ~I_mask)[VI_mask]) + offset, axis=2)
+    th_out, I_out = th_out[:, :, offset:], I_out[:, :, offset:]
+    return TimeEvolutionResult(problem, th_out if problem.store_theta else None,
+                               I_out if problem.store_current else None, V)
+
+
+class ThetaNotStored(Exception):
+    pass
+
+
+class CurrentNotStored(Exception):
+    pass
+
+
+class VoltageNotStored(Exception):
+    pass
+
+
+class DataAtTimepointNotStored(Exception):
+    pass
+
+
+class TimeEvolutionResult:
+    """Stored theta / current / voltage of a time evolution (time_evolution.py:597-1067)."""
+
+    def __init__(self, problem, theta, current, voltage):
+        self.problem = problem
+        Nj, W, Nt_s = problem.circuit._Nj(), problem.get_problem_count(), problem._Nt_s()
+        for name, arr, flag in (("theta", theta, problem.store_theta), ("current", current, problem.store_current),
+                                ("voltage", voltage, problem.store_voltage)):
+            if flag and arr.shape != (Nj, W, Nt_s):
+                raise ValueError(f"{name} must have shape {(Nj, W, Nt_s)}; has shape {arr.shape}")
+        self.theta = theta if problem.store_theta else None
+        self.current = current if problem.store_current else None
+        self.voltage = voltage if problem.store_voltage else None
+        s = problem.store_time_steps.astype(int)
+        self.time_point_indices = np.cumsum(s) - s
+
+    def get_problem_count(self):
+        return self.problem.get_problem_count()
+
+    def get_circuit(self):
+        return self.problem.get_circuit()
+
+    def _time_point_index(self, time_points):
+        if time_points is None:
+            time_points = self.problem.store_time_steps
+        if not np.all(self.problem.store_time_steps[time_points]):
+            raise DataAtTimepointNotStored("Queried a timepoint that is not stored during time evolution simulation.")
+        return self.time_point_indices[time_points]
+
+    def _th(self, tp):
+        if self.theta is None:
+            raise ThetaNotStored("Cannot query theta; quantity is not stored during time evolution simulation.")
+        return self.theta[:, :, self._time_point_index(tp)]
+
+    def _V(self, tp):
+        if self.voltage is None:
+            raise VoltageNotStored("Cannot query voltage; quantity is not stored during time evolution simulation.")
+        return self.voltage[:, :, self._time_point_index(tp)]
+
+    def _I(self, tp):
+        if self.current is None:
+            raise CurrentNotStored("Cannot query current; quantity is not stored during time evolution simulation.")
+        return self.current[:, :, self._time_point_index(tp)]
+
+    def _select(self, select_time_points, N, func):
+        sel = np.flatnonzero(self.problem._to_time_point_mask(select_time_points))
+        out = np.zeros((N, self.get_problem_count(), len(sel)), dtype=np.double)
+        for k, tp in enumerate(sel):
+            out[:, :, k] = func(tp)
+        return out
+
+    def get_theta(self, select_time_points=None):
+        return self._select(select_time_points, self.get_circuit()._Nj(), self._th)
+
+    def get_current(self, select_time_points=None):
+        return self._select(select_time_points, self.get_circuit()._Nj(), self._I)
+
+    def get_voltage(self, select_time_points=None):
+        return self._select(select_time_points, self.get_circuit()._Nj(), self._V)
+
+    def get_vortex_configuration(self, select_time_points=None):
+        A = self.get_circuit().get_cycle_matrix()
+        func = lambda tp: -A @ np.round(self._th(tp) / (2.0 * np.pi))
+        try:
+            return self._select(select_time_points, self.get_circuit()._Nf(), func).astype(int)
+        except ThetaNotStored:
+            raise ThetaNotStored("Cannot compute n; requires theta to be stored in TimeEvolutionConfig")

@@ -1,0 +1,218 @@
+"""Generate the golden fixtures under tests/golden/ by running the reference pyjjasim.
+
+This script is the only committed code that imports the reference package. It runs
+in a container that has the reference sources mounted at /root/reference (read-only);
+the fixtures it writes (`*.npz`) are what the tests read on machines without it.
+
+Import recipe: the reference imports itself as ``pyjjasim.*`` (pyjjasim/__init__.py),
+imports matplotlib at module load (embedded_graph.py:3-4, circuit_visualize.py:3-11),
+and calls ``np.asscalar`` (time_evolution.py:322), which numpy removed. So the script
+puts a symlink ``pyjjasim -> /root/reference`` in a temporary directory on sys.path,
+stubs the matplotlib modules and re-adds ``np.asscalar``. Nothing in the reference is
+modified; bytecode writing is disabled so its read-only tree is never touched.
+
+Each fixture holds the exact inputs (cycle matrix A, component vectors, source arrays or
+the parameters of a source callable, seeds, store masks) and the reference outputs
+(theta, current, voltage at the stored steps, and the vortex configuration), so a test
+can rebuild the same problem with no reference present.
+
+Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+"""
+import argparse
+import os
+import sys
+import tempfile
+import types
+import warnings
+
+import numpy as np
+import scipy.sparse
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def import_reference(ref_dir):
+    for m in ["matplotlib", "matplotlib.pyplot", "matplotlib.collections", "matplotlib.animation",
+              "matplotlib.colors", "matplotlib.cm", "matplotlib.patches", "matplotlib.lines",
+              "matplotlib.legend_handler", "matplotlib.text"]:
+        mod = types.ModuleType(m)
+        mod.__getattr__ = lambda name: (lambda *a, **k: None)
+        sys.modules[m] = mod
+    if not hasattr(np, "asscalar"):
+        np.asscalar = lambda a: a.item()
+    sys.dont_write_bytecode = True
+    tmp = tempfile.mkdtemp(prefix="pyjjasim_ref_")
+    os.symlink(ref_dir, os.path.join(tmp, "pyjjasim"))
+    sys.path.insert(0, tmp)
+    warnings.filterwarnings("ignore", category=SyntaxWarning)
+    import pyjjasim  # noqa: F401
+    return pyjjasim
+
+
+def csr_parts(prefix, M):
+    M = scipy.sparse.csr_matrix(M)
+    M.sort_indices()
+    return {prefix + "_data": M.data.astype(np.float64), prefix + "_indices": M.indices.astype(np.int64),
+            prefix + "_indptr": M.indptr.astype(np.int64), prefix + "_shape": np.array(M.shape, np.int64)}
+
+
+def circuit_parts(c):
+    d = {}
+    d.update(csr_parts("A", c.get_cycle_matrix()))
+    d.update(csr_parts("M", c.get_cut_matrix()))
+    d.update(csr_parts("L", c.get_inductance()))
+    x, y = c.get_node_coordinates()
+    n1, n2 = c.get_junction_nodes()
+    d.update(Ic=c.get_critical_current().copy(), R=c.get_resistance().copy(),
+             C=c.get_capacitance().copy(), node_x=np.asarray(x, np.float64), node_y=np.asarray(y, np.float64),
+             node1=np.asarray(n1, np.int64), node2=np.asarray(n2, np.int64),
+             face_centroid_x=np.asarray(c.get_face_centroids()[0], np.float64),
+             face_centroid_y=np.asarray(c.get_face_centroids()[1], np.float64))
+    return d
+
+
+def run_case(pj, name, circuit, dt, Nt, *, f=0.0, Is=0.0, Vs=0.0, T=0.0, seed=None, store=None,
+             stencil_width=3, th_m1=None, th_m2=None, th_m3=None, th_m4=None, Is_spec=None, extra=None):
+    """Run the reference compute() and save inputs + outputs."""
+    kw = dict(time_step=dt, time_step_count=Nt, external_flux=f, current_sources=Is, voltage_sources=Vs,
+              temperature=T, store_time_steps=store, stencil_width=stencil_width,
+              config_at_minus_1=th_m1, config_at_minus_2=th_m2, config_at_minus_3=th_m3,
+              config_at_minus_4=th_m4)
+    prob = pj.TimeEvolutionProblem(circuit, **kw)
+    if seed is not None:
+        np.random.seed(seed)
+    res = prob.compute()
+    W = prob.get_problem_count()
+    d = circuit_parts(circuit)
+    d.update(dt=np.float64(dt), Nt=np.int64(Nt), W=np.int64(W), stencil_width=np.int64(stencil_width),
+             seed=np.int64(-1 if seed is None else seed), store_mask=prob.get_store_time_steps().copy(),
+             theta=res.get_theta(), current=res.current.copy(), voltage=res.get_voltage(),
+             vortex=res.get_vortex_configuration())
+    # inputs: arrays stored compact (before broadcasting); callables by their parameters
+    for key, val in (("f", f), ("Is", Is), ("Vs", Vs), ("T", T)):
+        if callable(val):
+            continue
+        d["in_" + key] = np.array(val, dtype=np.float64)
+    for key, val in (("th_m1", th_m1), ("th_m2", th_m2), ("th_m3", th_m3), ("th_m4", th_m4)):
+        if val is not None:
+            d["in_" + key] = np.array(val, dtype=np.float64)
+    if Is_spec is not None:
+        for k, v in Is_spec.items():
+            d["Is_spec_" + k] = np.asarray(v)
+    if extra:
+        d.update(extra)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **d)
+    print(f"{name}: Nj={circuit.junction_count()} Nf={circuit.face_count()} W={W} Nt={Nt} -> "
+          f"{os.path.getsize(path) / 1024:.0f} KB")
+
+
+def every(Nt, k):
+    m = np.zeros(Nt, bool)
+    m[::k] = True
+    m[-1] = True
+    return m
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    pj = import_reference(args.ref)
+
+    # Lattice fixtures: cycle matrices, cut matrices and current_base for the three lattice kinds.
+    lat = {}
+    for kind, cls, sizes in (("square", pj.SquareArray, [(2, 2), (3, 3), (4, 7), (10, 10), (7, 4)]),
+                             ("honeycomb", pj.HoneycombArray, [(1, 1), (2, 2), (3, 4), (4, 3)]),
+                             ("triangular", pj.TriangularArray, [(2, 2), (3, 3), (4, 5), (5, 4)])):
+        for (nx, ny) in sizes:
+            c = cls(nx, ny)
+            key = f"{kind}_{nx}x{ny}"
+            for k, v in circuit_parts(c).items():
+                lat[key + "__" + k] = v
+            lat[key + "__cb0"] = c.current_base(0.0)
+            lat[key + "__cb90"] = c.current_base(np.pi / 2)
+            lat[key + "__cb30"] = c.current_base(np.pi / 6)
+    np.savez_compressed(os.path.join(HERE, "lattices.npz"), **lat)
+    print("lattices.npz written")
+
+    # Config 1 exactly: SquareArray(10,10), f=0.1, Is=0.5*current_base(0), T=0, dt=0.05, 2000 steps.
+    a = pj.SquareArray(10, 10)
+    Is = 0.5 * a.current_base(0.0)
+    run_case(pj, "c1_square10_dc", a, 0.05, 2000, f=0.1, Is=Is[:, None, None], store=every(2000, 25))
+
+    # Config 2 shape, reduced: C=1, L=0.1, AC bias callable, T=0.01, seeded noise (Nj <= 500: fresh draws).
+    a = pj.SquareArray(8, 8)
+    a.set_capacitance(1.0)
+    a.set_inductance(0.1)
+    base = a.current_base(0.0)
+    dt = 0.05
+    Is_fn = lambda i: (base * (0.8 + 0.3 * np.sin(2 * np.pi * 0.05 * i * dt)))[:, None]
+    run_case(pj, "c2_square8_cl_ac_noise", a, dt, 400, f=0.1, Is=Is_fn, T=0.01, seed=0,
+             store=every(400, 10), Is_spec=dict(base=base, dc=0.8, ac=0.3, freq=0.05))
+
+    # Config 3 shape, reduced: W=8 IV sweep, f=0.25, bias linspace(0, 2, 8), T=0.
+    a = pj.SquareArray(12, 12)
+    Is = a.current_base(0.0)[:, None, None] * np.linspace(0, 2, 8)[None, :, None]
+    run_case(pj, "c3_square12_iv_w8", a, 0.05, 600, f=0.25, Is=Is, store=every(600, 50))
+
+    # Nj > 500: the reference reuses the previous draw with permuted rows on steps i % 3 != 0.
+    a = pj.SquareArray(17, 17)
+    Is = 0.5 * a.current_base(0.0)
+    run_case(pj, "c4_square17_noise_perm", a, 0.05, 30, f=0.1, Is=Is[:, None, None] * np.array([1.0, 0.6])[None, :, None],
+             T=0.02, seed=3, store=every(30, 4))
+
+    # Config 4 shape, reduced: lognormal Ic, bias 1.2, W=4 (Ic is per circuit, W shares it).
+    rng = np.random.default_rng(7)
+    a = pj.SquareArray(8, 8)
+    a.set_critical_current(rng.lognormal(0.0, 0.2, a.junction_count()))
+    Is = 1.2 * a.current_base(0.0)
+    run_case(pj, "c5_square8_lognormal_ic", a, 0.05, 500, f=np.array([0.1, 0.15, 0.2, 0.3])[None, :, None],
+             Is=Is[:, None, None], store=every(500, 25))
+
+    # Honeycomb and triangular lattices.
+    a = pj.HoneycombArray(4, 3)
+    Is = 0.7 * a.current_base(0.0)
+    run_case(pj, "c6_honeycomb4x3", a, 0.05, 300, f=0.2, Is=Is[:, None, None] * np.array([1.0, 1.5])[None, :, None],
+             store=every(300, 10))
+    a = pj.TriangularArray(5, 4)
+    Is = 0.6 * a.current_base(0.0)
+    run_case(pj, "c7_triangular5x4", a, 0.05, 300, f=0.15, Is=Is[:, None, None], store=every(300, 10))
+
+    # Stencil widths 4 and 5, with capacitance and voltage sources (theta_s path).
+    for sw in (4, 5):
+        a = pj.SquareArray(6, 6)
+        a.set_capacitance(0.5)
+        Nj = a.junction_count()
+        rng = np.random.default_rng(sw)
+        Vs = 0.01 * rng.standard_normal(Nj)
+        Is = 0.4 * a.current_base(0.0)
+        th0 = 0.1 * rng.standard_normal(Nj)
+        run_case(pj, f"c8_square6_stencil{sw}_vs", a, 0.05, 200, f=0.1, Is=Is[:, None, None], Vs=Vs[:, None, None],
+                 store=every(200, 10), stencil_width=sw, th_m1=th0)
+
+    # Mutual inductance matrix and junction current sources not derived from node currents.
+    a = pj.SquareArray(6, 6)
+    Nj = a.junction_count()
+    rng = np.random.default_rng(11)
+    Lm = scipy.sparse.diags(np.full(Nj, 0.3)) + scipy.sparse.diags(np.full(Nj - 1, 0.05), 1) + \
+        scipy.sparse.diags(np.full(Nj - 1, 0.05), -1)
+    a.set_inductance(Lm.tocsc())
+    Is = 0.3 * rng.standard_normal(Nj)
+    run_case(pj, "c9_square6_mutual_l", a, 0.05, 200, f=0.05, Is=Is[:, None, None], store=every(200, 5))
+
+    # Time-dependent arrays for f and T (full (N, W, Nt) arrays), noise with time-dependent T, W=3.
+    a = pj.SquareArray(7, 5)
+    Nt = 120
+    Nf, Nj = a.face_count(), a.junction_count()
+    fa = 0.1 + 0.05 * np.sin(np.arange(Nt) * 0.1)[None, None, :] * np.ones((Nf, 3, 1))
+    Ta = np.linspace(0.0, 0.02, Nt)[None, None, :] * np.ones((1, 3, 1))
+    Is = 0.5 * a.current_base(0.0)
+    th1 = 0.2 * np.random.default_rng(5).standard_normal((Nj, 3))
+    th2 = th1 - 0.01
+    run_case(pj, "c10_square7x5_timedep", a, 0.1, Nt, f=fa, Is=Is[:, None, None], T=Ta, seed=9,
+             store=every(Nt, 3), th_m1=th1, th_m2=th2)
+
+
+if __name__ == "__main__":
+    main()
