@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""Benchmark: RCSJ time-evolution throughput (junction-steps/s) on one GB300.
+
+Workload (batched IV sweep): W = 512 copies of SquareArray(128, 128) (Nj = 32 512
+junctions, Nf = 16 129 faces), Ic = 1, R = 1, C = 0, L = 0, frustration f = 0.25, DC bias
+current_base(0) * linspace(0, 2, 512), T = 0, dt = 0.05, FP64. Synthetic inputs of exactly
+that shape (no dataset is involved). A bench "step" is one time step of all 512 problems.
+
+Reported (one JSON line):
+  value       junction-steps/s with the state resident on the device (CUDA events around
+              --steps graph-replayed steps on the launching stream);
+  e2e         the same metric through the public API, TimeEvolutionProblem(...).compute(),
+              host inputs in, host results out (copies inside the timed region);
+  plain_gpu   the same lattice, one problem per launch (W = 1);
+  roofline    the dominant stage (forward supernodal solve) against the FP64 pipe, with
+              its HBM figures beside it; stage times from CUDA events per stage;
+  cpu_baseline the CPU oracle (numpy/scipy restatement of the reference's loop) on a
+              bounded sample of the same workload, timed on this host.
+``--impl reference`` times the CPU oracle alone on the same workload (reference arm).
+Under torchrun (N > 1) every rank runs its own 512-problem slice of an N*512-point sweep
+(independent problems, no collective on the data path); ``value`` sums all ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX = NY = 128
+W_BATCH = 512
+FRUST = 0.25
+DT = 0.05
+METRIC = "junction-steps/s (batched IV sweep, SquareArray(128,128) x 512, FP64)"
+PROFILE_JSON = os.path.join(ROOT, "profiles", "traffic_iv_sweep_128x128_w512.json")
+
+
+def config(n_gpus):
+    return {"workload": "batched IV sweep: W=512 x SquareArray(128,128), Ic=1 R=1 C=0 L=0, f=0.25, "
+                        "DC bias linspace(0,2,512)*current_base(0), T=0, dt=0.05, FP64",
+            "Nj": 2 * NX * (NY - 1), "Nf": (NX - 1) * (NY - 1), "W_per_gpu": W_BATCH, "global_batch": W_BATCH * n_gpus,
+            "l2_policy": "inputs larger than L2: each (Nj, W) state array is 133 MB (> 129 MB L2)",
+            "parallelism": f"replicas x{n_gpus}" if n_gpus > 1 else "single GPU"}
+
+
+def bias_slice(rank, world, W=W_BATCH):
+    """Bias values of this rank: its contiguous W-slice of a world*W-point sweep over [0, 2]."""
+    allb = np.linspace(0.0, 2.0, W * world)
+    return allb[rank * W:(rank + 1) * W]
+
+
+def make_problem(mod, Nt, bias, store_last=True, W=None):
+    a = mod.SquareArray(NX, NY)
+    Is = a.current_base(0.0)[:, None, None] * np.asarray(bias)[None, :, None]
+    kw = dict(time_step=DT, time_step_count=Nt, current_sources=Is, external_flux=FRUST)
+    if store_last:
+        kw["store_time_steps"] = [Nt - 1]
+    return mod.TimeEvolutionProblem(a, **kw)
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.gpu_id, self.proc, self.lines = gpu_id, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu_id), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 peak of this GPU: cuBLAS DGEMM 4096^3, best of 5."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+def cpu_oracle_rate(W_sample, steps, warm=2):
+    """Per-step time of the CPU oracle on the full lattice with W_sample problems."""
+    import pyjjasim_gb300 as G
+    from oracle import rcsj_oracle
+    Nt = warm + steps
+    prob = make_problem(G, Nt, np.linspace(0.0, 2.0, W_sample), store_last=True)
+    stamps = {}
+
+    def on_step(i):
+        if i == warm - 1 or i == Nt - 1:
+            stamps[i] = time.perf_counter()
+
+    rcsj_oracle.evolve(prob, prob.store_time_steps, prob.store_time_steps, on_step=on_step)
+    per_step = (stamps[Nt - 1] - stamps[warm - 1]) / steps
+    Nj = prob.get_circuit()._Nj()
+    return Nj * W_sample / per_step, per_step
+
+
+def run_reference(args):
+    """Reference arm: the CPU oracle (restatement of the reference's loop, same library solve)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    t_est_full = None
+    # one step of the full batch takes seconds; size the per-step sample so the run stays short
+    import pyjjasim_gb300 as G
+    from oracle import rcsj_oracle
+    W_s = W_BATCH
+    probe_rate, probe_step = cpu_oracle_rate(16, 2, warm=1)
+    t_est_full = probe_step * W_BATCH / 16
+    budget = 150.0
+    if t_est_full * (args.steps + args.warmup) > budget:
+        W_s = int(max(8, min(W_BATCH, W_BATCH * budget / (t_est_full * (args.steps + args.warmup)))))
+    Nt = args.warmup + args.steps
+    prob = make_problem(G, Nt, np.linspace(0.0, 2.0, W_s), store_last=True)
+    stamps = {}
+
+    def on_step(i):
+        stamps[i] = time.perf_counter()
+
+    t_start = time.perf_counter()
+    rcsj_oracle.evolve(prob, prob.store_time_steps, prob.store_time_steps, on_step=on_step)
+    t0 = stamps[args.warmup - 1] if args.warmup > 0 else t_start
+    el = stamps[Nt - 1] - t0
+    Nj = prob.get_circuit()._Nj()
+    value = Nj * W_s * args.steps / el
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "junction-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (IV-sweep inputs generated in-process)", "config": config(1),
+            "cpu_baseline": {"value": value, "unit": "junction-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"one step = one time step of W={W_s} problems of the 512-point sweep "
+                                       f"(bias linspace(0,2,{W_s})) on the full 128x128 lattice; numpy/scipy "
+                                       f"restatement of the reference loop, SuperLU solve as in the reference"},
+            "e2e": {"value": value, "unit": "junction-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import pyjjasim_gb300 as G
+    from pyjjasim_gb300 import _native as N
+    from pyjjasim_gb300.backend import GpuSimulation
+
+    bias = bias_slice(rank, world)
+    Nt_total = args.warmup + args.steps
+    prob = make_problem(G, Nt_total, bias)
+    Nj, Nf, W = prob.get_circuit()._Nj(), prob.get_circuit()._Nf(), prob.get_problem_count()
+
+    t0 = time.perf_counter()
+    sim = GpuSimulation(prob)
+    sim.synchronize()
+    t_plan = time.perf_counter() - t0
+    fstats = None
+    from pyjjasim_gb300 import plan as P
+    for (f, _A) in P._FACTORS.values():
+        fstats = f.stats
+    # warm-up: at least one full graph length so the CUDA graph is captured before timing
+    sim.run(max(args.warmup, 64), use_graph=True)
+    sim.synchronize()
+    lib = N.lib()
+    props = torch.cuda.get_device_properties(local)
+    gpu_id = getattr(props, "uuid", None)
+    gpu_id = (str(gpu_id) if str(gpu_id).startswith("GPU-") else f"GPU-{gpu_id}") if gpu_id is not None else local
+    stream = sim.stream
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(gpu_id) as clk:
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        n0 = lib.jja_launch_count()
+        ev0.record(stream)
+        sim.run(args.steps, use_graph=True)
+        ev1.record(stream)
+        ev1.synchronize()
+        launches = lib.jja_launch_count() - n0
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+    el = ev0.elapsed_time(ev1) / 1e3
+    if world > 1:
+        t = torch.tensor([el], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el = float(t.item())
+    assert bool(torch.isfinite(sim.theta()).all()), "non-finite state"
+    value = Nj * W * args.steps * world / el
+    clocks = clk.summary()
+    # graph replays are counted at capture time only: count the kernels of one eager step
+    n1 = lib.jja_launch_count()
+    sim.run(1, use_graph=False)
+    sim.synchronize()
+    per_step_launches = lib.jja_launch_count() - n1
+    gpu_launches = per_step_launches * args.steps
+
+    # per-stage device time (eager, CUDA events at the stage boundaries of every step)
+    stages = sim.run_timed(args.steps)
+    stage_share = {k: v / stages["total"] for k, v in stages.items() if k != "total"}
+
+    line = {"metric": METRIC, "value": value, "unit": "junction-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (IV-sweep inputs generated in-process)", "config": config(world),
+            "gpu_launches": int(gpu_launches), "clocks": clocks,
+            "plan_seconds": t_plan, "factor": fstats}
+    if rank == 0:
+        # roofline of the dominant stage (forward supernodal solve; backward is its mirror)
+        nnzL = fstats["nnz_L"]
+        fwd_s = stages["forward"] / 1e3 / args.steps
+        fwd_flops = 2.0 * nnzL * W
+        fwd_bytes = 16.0 * Nf * W + 8.0 * fstats["f_values"]
+        peaks = measured_peaks()
+        fp64 = fp64_peak_tflops(torch)
+        traffic = None
+        try:
+            with open(PROFILE_JSON) as fh:
+                traffic = json.load(fh).get("forward_sweep_dram_bytes_per_step")
+        except Exception:
+            traffic = None
+        hbm_peak = peaks.get("hbm_gbs", 6800.0)
+        line["roofline"] = {
+            "kernel": "forward supernodal solve (k_fwd_level, all levels of one step)",
+            "bound": "fp64", "achieved": fwd_flops / fwd_s / 1e12, "peak": fp64, "unit": "TFLOP/s",
+            "frac": (fwd_flops / fwd_s / 1e12) / fp64,
+            "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (FP64 has no entry in MEASURED_PEAKS.json)",
+            "traffic": traffic,
+            "algorithmic_flops_per_launch": fwd_flops, "algorithmic_bytes_per_launch": fwd_bytes,
+            "hbm": {"achieved": fwd_bytes / fwd_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": fwd_bytes / fwd_s / 1e9 / hbm_peak,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s"},
+            "stage_ms_per_step": {k: v / args.steps for k, v in stages.items()},
+            "stage_share": stage_share}
+        # plain GPU path: one problem per launch
+        prob1 = make_problem(G, 1, [1.0])
+        sim1 = GpuSimulation(prob1)
+        sim1.run(max(args.warmup, 40), use_graph=True)
+        sim1.synchronize()
+        k1 = max(args.steps, 200)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(sim1.stream)
+        sim1.run(k1, use_graph=True)
+        e1.record(sim1.stream)
+        e1.synchronize()
+        t1 = e0.elapsed_time(e1) / 1e3
+        plain = Nj * k1 / t1
+        line["plain_gpu"] = {"value": plain, "unit": "junction-steps/s", "W": 1, "ms_per_step": t1 / k1 * 1e3,
+                             "batched_over_plain": value / world / plain}
+        del sim1
+        # end to end through the public API with host buffers
+        if not args.no_e2e:
+            pe = make_problem(G, args.steps, bias)
+            pe.compute()                                  # warm: plan cache, graph capture
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = pe.compute()
+            th = res.get_theta()
+            t_e2e = time.perf_counter() - t0
+            assert np.isfinite(th).all()
+            stored = (pe.store_time_steps | np.roll(pe.store_time_steps, -1))  # V needs the previous step
+            h2d = (2 * Nj * W + Nj * W) * 8 + 8           # theta(t-1), theta(t-2), Is (Nj x W), f (scalar)
+            d2h = (int(stored.sum()) + int(pe.store_time_steps.sum())) * Nj * W * 8
+            line["e2e"] = {"value": Nj * W * args.steps / t_e2e, "unit": "junction-steps/s",
+                           "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+                           "time_steps_per_call": args.steps, "seconds_per_call": t_e2e,
+                           "api": "pyjjasim_gb300.TimeEvolutionProblem(...).compute()"}
+        if not args.no_cpu_baseline:
+            rate, per_step = cpu_oracle_rate(W_BATCH, 6)
+            line["cpu_baseline"] = {"value": rate, "unit": "junction-steps/s", "cores": os.cpu_count(),
+                                    "kind": "port", "seconds_per_step": per_step,
+                                    "sample": "6 time steps of the full W=512 batch (after 2 warm steps), "
+                                              "numpy/scipy oracle restating the reference loop; SuperLU solve; "
+                                              "numpy single-threaded, BLAS threads default"}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

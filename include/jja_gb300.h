@@ -1,0 +1,148 @@
+/*
+ * jja_gb300.h — C ABI of the GB300 (sm_103a) RCSJ time-stepping library libjja_gb300.so.
+ *
+ * The reference (pyjjasim) has no native layer: its hot path is the Python function
+ * time_evolution_core(problem, th_store_mask, I_store_mask) (time_evolution.py:461-582),
+ * called by time_evolution() (:443) from TimeEvolutionProblem.compute() (:303-307).
+ * These entry points replace the pieces of that function; the ctypes binding in
+ * pyjjasim_gb300/_native.py (and the stub in INTEGRATION.md) call them.
+ *
+ * Conventions: plain pointers and sizes, no framework types. Functions return 0 on success
+ * and a nonzero jja_status otherwise; jja_last_error() gives the message (per thread).
+ * "device" pointers are CUDA global-memory pointers on the current device; "host" pointers
+ * are ordinary memory. Arrays indexed (j, w) are row-major with the problem index w
+ * contiguous: element (j, w) is at j*W + w (the reference's (Nj, W) layout).
+ */
+#ifndef JJA_GB300_H
+#define JJA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  JJA_OK = 0,
+  JJA_ERR_ARG = 1,        /* invalid argument / shape */
+  JJA_ERR_NOT_SPD = 2,    /* face-space matrix is not positive definite */
+  JJA_ERR_CUDA = 3,       /* a CUDA runtime call failed */
+  JJA_ERR_NONFINITE = 4,  /* NaN/Inf detected in the state */
+  JJA_ERR_INTERNAL = 5
+} jja_status;
+
+typedef struct jja_factor jja_factor;
+typedef struct jja_plan jja_plan;
+
+/* ---------------------------------------------------------------- host factorisation --- */
+
+typedef struct {
+  int nd_leaf;        /* nested-dissection leaf size (<= 0: default 8) */
+  int max_supernode;  /* cap on supernode width (0: none) */
+  int keep_factor;    /* keep plain Cholesky columns for host checks */
+} jja_factor_opts;
+
+typedef struct {
+  int n;              /* matrix order (faces) */
+  int n_supernodes;
+  int n_levels;       /* levels of the supernodal elimination tree */
+  int max_k, max_m;   /* widest supernode, longest off-diagonal row list */
+  int64_t nnz_L;      /* nonzeros of L (supernodal, lower triangle incl. diagonal) */
+  int64_t f_values;   /* doubles in the (k+m) x k solve blocks */
+  double factor_flops;
+} jja_factor_stats;
+
+/* Orders and factorises the face-space matrix K = A (L + diag(1/c0)) A^T
+ * (time_evolution.py:504-506, where the reference calls scipy.sparse.linalg.factorized).
+ * K: n x n symmetric, full pattern (both triangles), CSC with 64-bit column pointers.
+ * coord_x/y: optional face coordinates (centroids) that seed the nested dissection; NULL to
+ * derive coordinates from breadth-first distances. perm: optional fill-reducing order
+ * (new -> old) that replaces the nested dissection. Runs on the host; no GPU needed. */
+int jja_factor_create(int n, const int64_t* colptr, const int32_t* rowind, const double* val,
+                      const double* coord_x, const double* coord_y, const int32_t* perm,
+                      const jja_factor_opts* opts, jja_factor** out);
+void jja_factor_destroy(jja_factor* f);
+int jja_factor_get_stats(const jja_factor* f, jja_factor_stats* out);
+/* perm_out[n]: new -> old face order used by the factor (a postordered nested dissection). */
+int jja_factor_get_perm(const jja_factor* f, int32_t* perm_out);
+/* Host solve K x = b in place (b: n x nrhs row-major, original order). Diagnostic only:
+ * used to check a factor without a GPU; the time-stepping path solves on the GPU. */
+int jja_factor_solve_host(const jja_factor* f, double* b, int nrhs);
+
+/* ------------------------------------------------------------------------ GPU plan --- */
+
+typedef struct {
+  int Nj, Nf, W;           /* junctions, faces, problems per launch */
+  int stencil_width;       /* 3, 4 or 5 (time_evolution.py:401-408) */
+  /* cycle matrix A (Nf x Nj, entries +-1) as CSR over the original face order */
+  const int64_t* a_rowptr; /* Nf+1 */
+  const int32_t* a_col;    /* junction index */
+  const double* a_val;     /* +1 / -1 */
+  /* per-junction coefficients (host arrays of length Nj) */
+  const double* Ic;        /* critical current (DefaultCPR: Ic sin(theta)) */
+  const double* inv_c0;    /* 1 / c0, c0 = s1[0] Rv + s2[0] Cv (time_evolution.py:477) */
+  const double* coef;      /* (stencil_width-1) x Nj: c_k = s1[k] Rv + s2[k] Cv, k = 1.. */
+  const double* Rv;        /* 1 / (dt R), noise amplitude sqrt(2 T Rv) (time_evolution.py:537) */
+  double extrap[4];        /* CPR argument weights on theta(t-1), theta(t-2), ... (:547-553) */
+  double dt;
+} jja_plan_desc;
+
+/* Uploads the circuit tables and the factor to the current CUDA device and allocates the
+ * face-space work vectors for W problems (cudaMalloc). The factor may be destroyed after. */
+int jja_plan_create(const jja_plan_desc* desc, const jja_factor* f, jja_plan** out);
+void jja_plan_destroy(jja_plan* p);
+/* Bytes of device memory held by the plan (tables + factor + work vectors). */
+int64_t jja_plan_device_bytes(const jja_plan* p);
+
+/* A per-step source on the device: value(n, w) = ptr[n*stride_n + w*stride_w]
+ * (element strides; 0 broadcasts). ptr == NULL means the source is identically zero. */
+typedef struct {
+  const double* ptr;
+  int64_t stride_n;
+  int64_t stride_w;
+} jja_view;
+
+enum { JJA_NOISE_NONE = 0, JJA_NOISE_BUFFER = 1, JJA_NOISE_PHILOX = 2 };
+
+typedef struct {
+  double* hist[4];       /* device (Nj x W): theta at t-1, t-2, ... (stencil_width-1 used);
+                            jja_run rotates them: on return hist[0] is the newest phase */
+  double* theta_s;       /* device (Nj x W) accumulated voltage-source phase, or NULL */
+  jja_view Is;           /* current sources (Nj rows) */
+  jja_view f;            /* external flux (Nf rows, original face order) */
+  jja_view Vs;           /* voltage sources (Nj rows) */
+  jja_view T;            /* temperature (Nj rows) */
+  int noise_mode;        /* JJA_NOISE_* */
+  const double* noise;   /* JJA_NOISE_BUFFER: device (Nj x W) standard normals of this step */
+  uint64_t seed;         /* JJA_NOISE_PHILOX: key */
+  int64_t step;          /* index of the first step of the call (Philox counter) */
+  double* th_out;        /* device (slots x Nj x W) or NULL */
+  double* I_out;         /* device (slots x Nj x W) or NULL */
+} jja_state;
+
+/* Runs nsteps time steps of the RCSJ update (time_evolution.py:523-580) on `stream`
+ * (a cudaStream_t, NULL = default stream). th_slot[i] / I_slot[i] (host arrays of length
+ * nsteps, or NULL) give the output slot of step i or -1. With use_graph != 0 the step
+ * sequence is captured once into a CUDA graph and replayed. */
+int jja_run(jja_plan* p, jja_state* st, int nsteps, const int64_t* th_slot, const int64_t* I_slot,
+            int use_graph, void* stream);
+
+/* Like jja_run (no stored outputs, no graph) but records CUDA events at the stage boundaries
+ * of every step. stage_ms[6] receives the summed device time of: junction currents,
+ * face right-hand side, forward solve, backward solve, update; and [5] the whole run.
+ * Used by the benchmark to attribute step time to kernels; same results as jja_run. */
+int jja_run_timed(jja_plan* p, jja_state* st, int nsteps, double* stage_ms, void* stream);
+
+/* Face-space solve on the device: x = K^{-1} b for W right-hand sides (device arrays
+ * Nf x W, original face order). Exposed for tests of the triangular-solve kernels. */
+int jja_solve(jja_plan* p, const double* b, double* x, void* stream);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* jja_last_error(void);
+/* Number of kernel launches the library issued since load (for launch accounting). */
+int64_t jja_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JJA_GB300_H */

@@ -60,12 +60,13 @@ class NumpyGlobalNoise:
         return self.prev
 
 
-def evolve(problem, th_store_mask, I_store_mask, noise=None):
+def evolve(problem, th_store_mask, I_store_mask, noise=None, on_step=None):
     """Restatement of time_evolution_core (time_evolution.py:461-582).
 
     Returns (th_out, I_out) of shape (Nj, W, sum(mask) + width - 1); slots
     0..width-2 hold the initial conditions (theta and cp(theta)), oldest first.
     ``noise``: callable i -> (Nj, W) standard normals; default NumpyGlobalNoise.
+    ``on_step``: optional callable(i) run after step i (used to time the loop).
     """
     c = problem.get_circuit()
     Nj, W, dt = c._Nj(), problem.get_problem_count(), problem._dt()
@@ -138,6 +139,8 @@ def evolve(problem, th_store_mask, I_store_mask, noise=None):
         if not Vs_zero:
             theta_s = theta_s + Vs * dt                                # :579-580
         hist = [th_next] + hist[:-1]
+        if on_step is not None:
+            on_step(i)
     return th_out, I_out
 
 

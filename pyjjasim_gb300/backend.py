@@ -1,0 +1,272 @@
+"""GPU replacement of the reference's time-stepping core.
+
+``time_evolution_core(problem, th_store_mask, I_store_mask)`` has the signature, inputs
+and outputs of pyjjasim's ``time_evolution_core`` (time_evolution.py:461-582): it reads
+the problem through the same accessors, and returns (th_out, I_out) as float64 arrays of
+shape (Nj, W, sum(mask) + stencil_width - 1) whose first stencil_width-1 slots hold the
+initial conditions (theta and cp(theta)), followed by the stored steps in order.
+
+The per-step work runs in libjja_gb300 on the GPU; this module only stages inputs, keeps
+device buffers (torch tensors, used as device memory) and copies results back. There is no
+CPU path: without a CUDA device or the built library the call raises.
+
+Noise. ``noise="numpy"`` consumes the global ``np.random`` state in the reference's call
+order (a fresh ``randn(Nj, W)`` per step, or for Nj > 500 one every third step with
+permuted rows in between, time_evolution.py:533-538), uploads each draw, and reproduces the
+reference's noisy trajectories. ``noise="philox"`` (default) draws fresh normals per
+junction, problem and step on the device (Philox4x32-10); its seed defaults to one 63-bit
+draw from ``np.random`` so ``np.random.seed`` still makes runs reproducible.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+from . import plan as P
+
+_MAX_OUT_BYTES = 8 << 30   # device bytes for stored steps per segment
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("pyjjasim_gb300 needs a CUDA GPU (GB300, sm_103a); none is available")
+    return torch
+
+
+def _is_default_cpr(cpr):
+    return type(cpr).__name__ == "DefaultCPR"
+
+
+class _Source:
+    """A source (Is, f, Vs or T) on the device as a strided view, updated per step if time-dependent."""
+
+    def __init__(self, torch, dev, stream, getter, timedep, N_rows, W, zero):
+        self.getter, self.timedep, self.N, self.W = getter, timedep, N_rows, W
+        self.zero = zero
+        self.buf = None
+        self.view = N.View(None, 0, 0)
+        self.h2d_bytes = 0
+        if zero:
+            return
+        v0 = np.broadcast_to(np.asarray(getter(0), dtype=np.float64), (N_rows, W))
+        if timedep:
+            rows, cols = N_rows, W        # a later step may not broadcast like step 0: keep it full
+        else:
+            rows = 1 if v0.strides[0] == 0 else N_rows
+            cols = 1 if v0.strides[1] == 0 else W
+        self.shape = (rows, cols)
+        self.buf = torch.empty(self.shape, dtype=torch.float64, device=dev)
+        self.view = N.View(self.buf.data_ptr(), cols if rows > 1 else 0, 1 if cols > 1 else 0)
+        self.torch, self.stream = torch, stream
+        self.load(0, v0)
+
+    def load(self, i, value=None):
+        if self.zero:
+            return
+        v = np.broadcast_to(np.asarray(self.getter(i) if value is None else value, np.float64), (self.N, self.W))
+        r, c = self.shape
+        host = np.ascontiguousarray(v[:r, :c])
+        with self.torch.cuda.stream(self.stream):
+            self.buf.copy_(self.torch.from_numpy(host))
+        self.h2d_bytes += host.nbytes
+
+
+class _NumpyNoise:
+    """Standard normals in the reference's np.random call order (time_evolution.py:533-538)."""
+
+    def __init__(self, Nj, W):
+        self.Nj, self.W, self.prev = Nj, W, None
+
+    def __call__(self, i):
+        if self.Nj > 500:
+            if i % 3 == 0:
+                self.prev = np.random.randn(self.Nj, self.W)
+            else:
+                self.prev = self.prev[np.random.permutation(self.Nj), :]
+        else:
+            self.prev = np.random.randn(self.Nj, self.W)
+        return self.prev
+
+
+class GpuSimulation:
+    """Device-resident state of W time-evolution problems of one TimeEvolutionProblem.
+
+    Holds the cached plan, the phase history, theta_s and the sources on the GPU. ``run``
+    advances any number of steps (optionally storing steps into device output buffers),
+    ``run_timed`` advances with per-stage CUDA-event timing, ``theta`` returns the newest phase.
+    """
+
+    def __init__(self, problem, noise="philox", seed=None, device=None, nd_leaf=8, stream=None):
+        torch = self.torch = _torch()
+        c = problem.get_circuit()
+        if not _is_default_cpr(problem.get_current_phase_relation()):
+            raise NotImplementedError("the GPU core evaluates the default current-phase relation Ic*sin(theta) only")
+        self.problem = problem
+        self.Nj, self.Nf, self.W = c._Nj(), c._Nf(), problem.get_problem_count()
+        self.width = problem.stencil_width
+        self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.h2d_bytes = 0
+        with torch.cuda.device(self.dev):
+            self.stream = stream if stream is not None else torch.cuda.Stream(device=self.dev)
+            self.plan = P.get_plan(c, problem._dt(), self.W, self.width, problem.stencil, nd_leaf=nd_leaf)
+            hist0 = [problem.config_at_minus_1, problem.config_at_minus_2]
+            if self.width >= 4:
+                hist0.append(problem.config_at_minus_3)
+            if self.width >= 5:
+                hist0.append(problem.config_at_minus_4)
+            self.hist0 = hist0
+            with torch.cuda.stream(self.stream):
+                host = [np.ascontiguousarray(np.broadcast_to(h, (self.Nj, self.W)), np.float64) for h in hist0]
+                self.hist = [torch.from_numpy(h).to(self.dev) for h in host]
+                self.h2d_bytes += sum(h.nbytes for h in host)
+
+            def is_zero(timedep, getter):     # zero detection as in time_evolution.py:509-519
+                return (not timedep) and bool(np.allclose(getter(0), 0))
+
+            self.srcs = {}
+            for name, getter, td, rows in (("Is", problem._Is, problem._Is_is_timedep, self.Nj),
+                                           ("f", problem._f, problem._f_is_timedep, self.Nf),
+                                           ("Vs", problem._Vs, problem._Vs_is_timedep, self.Nj),
+                                           ("T", problem._T, problem._T_is_timedep, self.Nj)):
+                self.srcs[name] = _Source(torch, self.dev, self.stream, getter, td, rows, self.W, is_zero(td, getter))
+            self.h2d_bytes += sum(s.h2d_bytes for s in self.srcs.values())
+            Vs_zero, T_zero = self.srcs["Vs"].zero, self.srcs["T"].zero
+            self.theta_s = None if Vs_zero else torch.zeros((self.Nj, self.W), dtype=torch.float64, device=self.dev)
+            st = self.state = N.State()
+            for k in range(4):
+                st.hist[k] = self.hist[k].data_ptr() if k < len(self.hist) else None
+            st.theta_s = self.theta_s.data_ptr() if self.theta_s is not None else None
+            st.Is, st.f, st.Vs, st.T = (self.srcs[k].view for k in ("Is", "f", "Vs", "T"))
+            st.step = 0
+            self.noise_gen = None
+            self.noise_buf = None
+            if T_zero:
+                st.noise_mode = N.NOISE_NONE
+            elif callable(noise):
+                self.noise_gen = noise
+            elif noise == "numpy":
+                self.noise_gen = _NumpyNoise(self.Nj, self.W)
+            elif noise == "philox":
+                st.noise_mode = N.NOISE_PHILOX
+                st.seed = int(np.random.randint(0, 2 ** 63 - 1, dtype=np.int64)) if seed is None else int(seed)
+            else:
+                raise ValueError(f"unknown noise mode {noise!r}")
+            if self.noise_gen is not None:
+                st.noise_mode = N.NOISE_BUFFER
+                self.noise_buf = torch.empty((self.Nj, self.W), dtype=torch.float64, device=self.dev)
+                st.noise = self.noise_buf.data_ptr()
+            self.per_step_host = self.noise_gen is not None or any(s.timedep and not s.zero for s in self.srcs.values())
+
+    # ----------------------------------------------------------------------------------------
+    def run(self, nsteps, th_slot=None, I_slot=None, th_dev=None, I_dev=None, use_graph=True):
+        """Advance nsteps steps; step i writes th_dev[th_slot[i]] / I_dev[I_slot[i]] when >= 0."""
+        torch, st = self.torch, self.state
+        lib = N.lib()
+        st.th_out = th_dev.data_ptr() if th_dev is not None else None
+        st.I_out = I_dev.data_ptr() if I_dev is not None else None
+        th_slot = None if th_slot is None else np.ascontiguousarray(th_slot, np.int64)
+        I_slot = None if I_slot is None else np.ascontiguousarray(I_slot, np.int64)
+        h = ctypes.c_void_p(self.stream.cuda_stream)
+        if not self.per_step_host:
+            N.check(lib.jja_run(self.plan.handle, ctypes.byref(st), int(nsteps), N.ptr(th_slot, ctypes.c_int64),
+                                N.ptr(I_slot, ctypes.c_int64), int(use_graph), h))
+            return
+        for k in range(nsteps):
+            i = st.step
+            for s in self.srcs.values():
+                if s.timedep and not s.zero and i > 0:
+                    s.load(i)
+            if self.noise_gen is not None:
+                with torch.cuda.stream(self.stream):
+                    self.noise_buf.copy_(torch.from_numpy(np.ascontiguousarray(self.noise_gen(i), np.float64)))
+            N.check(lib.jja_run(self.plan.handle, ctypes.byref(st), 1,
+                                N.ptr(th_slot[k:k + 1], ctypes.c_int64) if th_slot is not None else None,
+                                N.ptr(I_slot[k:k + 1], ctypes.c_int64) if I_slot is not None else None, 0, h))
+
+    def run_timed(self, nsteps):
+        """Advance nsteps steps (eager) and return per-stage device milliseconds."""
+        if self.per_step_host:
+            raise ValueError("run_timed needs device-resident sources and on-device noise")
+        ms = np.zeros(6)
+        N.check(N.lib().jja_run_timed(self.plan.handle, ctypes.byref(self.state), int(nsteps), N.ptr(ms),
+                                      ctypes.c_void_p(self.stream.cuda_stream)))
+        return dict(zip(("junction", "face_rhs", "forward", "backward", "update", "total"), ms.tolist()))
+
+    def theta_ptr(self):
+        return self.state.hist[0]
+
+    def theta(self):
+        """Newest phase (Nj, W) as a device tensor view."""
+        for t in self.hist:
+            if t.data_ptr() == self.state.hist[0]:
+                return t
+        raise RuntimeError("history buffer not found")
+
+    def synchronize(self):
+        self.stream.synchronize()
+
+
+def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", seed=None, device=None,
+                        use_graph=True, nd_leaf=8, stream=None):
+    """GPU time-stepping core; see the module docstring for the contract."""
+    sim = GpuSimulation(problem, noise=noise, seed=seed, device=device, nd_leaf=nd_leaf, stream=stream)
+    torch = sim.torch
+    Nj, W, Nt, width = sim.Nj, sim.W, problem._Nt(), sim.width
+    th_store_mask = np.asarray(th_store_mask, bool)
+    I_store_mask = np.asarray(I_store_mask, bool)
+    n_init = width - 1
+    n_th, n_I = int(th_store_mask.sum()), int(I_store_mask.sum())
+    th_out = np.zeros((Nj, W, n_th + n_init))
+    I_out = np.zeros((Nj, W, n_I + n_init))
+    for lag, th in enumerate(sim.hist0):     # initial conditions (time_evolution.py:480-502)
+        th_out[:, :, n_init - 1 - lag] = th
+        I_out[:, :, n_init - 1 - lag] = problem._cp(th)
+    th_idx = np.where(th_store_mask, np.cumsum(th_store_mask) - 1, -1).astype(np.int64)
+    I_idx = np.where(I_store_mask, np.cumsum(I_store_mask) - 1, -1).astype(np.int64)
+    max_slots = max(1, _MAX_OUT_BYTES // (2 * Nj * W * 8))
+    with torch.cuda.device(sim.dev):
+        i0 = 0
+        while i0 < Nt:
+            # segment [i0, i1) holds at most max_slots stored steps of each kind on the device
+            i1, cnt_th, cnt_I = i0, 0, 0
+            while i1 < Nt:
+                a, b = int(th_store_mask[i1]), int(I_store_mask[i1])
+                if cnt_th + a > max_slots or cnt_I + b > max_slots:
+                    break
+                cnt_th, cnt_I, i1 = cnt_th + a, cnt_I + b, i1 + 1
+            base_th, base_I = int(th_store_mask[:i0].sum()), int(I_store_mask[:i0].sum())
+            seg_th = np.where(th_idx[i0:i1] >= 0, th_idx[i0:i1] - base_th, -1)
+            seg_I = np.where(I_idx[i0:i1] >= 0, I_idx[i0:i1] - base_I, -1)
+            th_dev = torch.empty((cnt_th, Nj, W), dtype=torch.float64, device=sim.dev) if cnt_th else None
+            I_dev = torch.empty((cnt_I, Nj, W), dtype=torch.float64, device=sim.dev) if cnt_I else None
+            sim.run(i1 - i0, seg_th, seg_I, th_dev, I_dev, use_graph=use_graph)
+            sim.synchronize()
+            if cnt_th:
+                th_out[:, :, n_init + base_th:n_init + base_th + cnt_th] = th_dev.cpu().numpy().transpose(1, 2, 0)
+            if cnt_I:
+                I_out[:, :, n_init + base_I:n_init + base_I + cnt_I] = I_dev.cpu().numpy().transpose(1, 2, 0)
+            del th_dev, I_dev
+            i0 = i1
+    return th_out, I_out
+
+
+def solve_faces(circuit, dt, b, stencil_width=3, nd_leaf=8):
+    """K^{-1} b on the GPU for (Nf, W) right-hand sides (the per-step face-space solve)."""
+    from .problem import stencil
+    torch = _torch()
+    b = np.ascontiguousarray(b, np.float64)
+    squeeze = b.ndim == 1
+    if squeeze:
+        b = b[:, None]
+    W = b.shape[1]
+    pl = P.get_plan(circuit, dt, W, stencil_width, stencil(stencil_width), nd_leaf=nd_leaf)
+    st = torch.cuda.Stream()
+    with torch.cuda.stream(st):
+        bd = torch.from_numpy(b).cuda()
+        xd = torch.empty_like(bd)
+    st.synchronize()
+    pl.solve(bd.data_ptr(), xd.data_ptr(), st.cuda_stream)
+    st.synchronize()
+    x = xd.cpu().numpy()
+    return x[:, 0] if squeeze else x

@@ -1,0 +1,696 @@
+// GB300 (sm_103a) RCSJ time-stepping kernels and the C ABI of libjja_gb300.so.
+//
+// One time step of the reference (pyjjasim time_evolution.py:523-580), for W problems at once:
+//   k_junction : x = sigma*xi - Is + Ic sin(sum_k e_k theta_k) + sum_k c_k theta_k   (:533-558)
+//   k_face_rhs : b = A (x/c0 - theta_s) - 2 pi f, written in the factor's face order (:560-569)
+//   k_fwd_level: forward supernodal solve, one launch per elimination-tree level
+//   k_bwd_level: backward supernodal solve, one launch per level (reverse order)
+//   k_update   : y = A^T J ; theta_next = (y - x)/c0 ; I = y + Is ; theta_s += Vs dt  (:570-580)
+// Layout: every (N, W) array is row-major with the problem index w contiguous, so a warp
+// reads 32 problems of one junction/face in one 256-byte transaction when W >= 32.
+#include "../../include/jja_gb300.h"
+#include "jja_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<int64_t> g_launches{0};
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define JJA_CUDA(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      throw Error(JJA_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));            \
+  } while (0)
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    f();
+    return JJA_OK;
+  } catch (const Error& e) {
+    g_err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return JJA_ERR_INTERNAL;
+  }
+}
+
+constexpr int kWarpsPerBlock = 4;   // level kernels: one warp per work item
+constexpr int kRowsPerLane = 4;     // rows of a work item handled by one lane
+constexpr double kTwoPi = 6.283185307179586;
+
+// ------------------------------------------------------------------------------------------
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3", SC 2011), used for on-device thermal noise.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += W0;
+    k.y += W1;
+  }
+  return c;
+}
+
+// one standard normal per (element, step) via Box-Muller in single precision; noise values
+// need no FP64 accuracy and GB300's FP32 pipe is far wider than its FP64 pipe
+__device__ __forceinline__ double philox_normal(uint64_t seed, uint64_t elem, uint64_t step) {
+  uint4 c = make_uint4((uint32_t)elem, (uint32_t)(elem >> 32), (uint32_t)step, (uint32_t)(step >> 32));
+  uint4 r = philox4x32_10(c, make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+  const float u1 = ((float)(r.x >> 8) + 1.0f) * (1.0f / 16777216.0f);  // (0, 1]
+  const float u2 = (float)(r.y >> 8) * (1.0f / 16777216.0f);           // [0, 1)
+  const float rad = sqrtf(-2.0f * logf(u1));
+  return (double)(rad * cospif(2.0f * u2));
+}
+
+__device__ __forceinline__ double view_at(const jja_view& v, int64_t n, int64_t w) {
+  return v.ptr ? __ldg(v.ptr + n * v.stride_n + w * v.stride_w) : 0.0;
+}
+
+struct StepArgs {
+  int Nj, Nf, W, width;
+  const double* h[4];
+  double* hout;
+  double* theta_s;
+  jja_view Is, f, Vs, T;
+  int noise_mode;
+  const double* noise;
+  uint64_t seed;
+  const int64_t* d_step;
+  int64_t th_slot, I_slot;
+  double* th_out;
+  double* I_out;
+  double e[4];
+  double dt;
+};
+
+struct Tables {
+  const double* Ic;
+  const double* inv_c0;
+  const double* coef;   // (width-1) x Nj
+  const double* Rv;
+  const int64_t* fj_ptr;   // permuted face -> junction entries
+  const int32_t* fj_col;
+  const double* fj_val;
+  const int32_t* face_orig;
+  const int32_t* jf_face;  // 2 per junction (permuted face or -1)
+  const double* jf_val;
+};
+
+// x(j, w) for this step (time_evolution.py:533-558)
+__global__ void __launch_bounds__(256) k_junction(StepArgs a, Tables t, double* __restrict__ xj) {
+  const int64_t NjW = (int64_t)a.Nj * a.W;
+  const int64_t step = a.d_step ? *a.d_step : 0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = e / a.W, w = e - j * a.W;
+    double arg = 0.0, X;
+    double th[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k < a.width - 1) { th[k] = a.h[k][e]; arg = fma(a.e[k], th[k], arg); }
+    X = __ldg(t.Ic + j) * sin(arg);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k < a.width - 1) X = fma(__ldg(t.coef + (int64_t)k * a.Nj + j), th[k], X);
+    double fl = 0.0;
+    if (a.noise_mode != JJA_NOISE_NONE) {
+      const double T = view_at(a.T, j, w);
+      const double xi = a.noise_mode == JJA_NOISE_BUFFER ? a.noise[e] : philox_normal(a.seed, (uint64_t)e, (uint64_t)step);
+      fl = sqrt(2.0 * T * __ldg(t.Rv + j)) * xi;
+    }
+    xj[e] = (fl - view_at(a.Is, j, w)) + X;
+  }
+}
+
+// b(p, w) = sum_j A_pj (x_j / c0_j - theta_s_j) - 2 pi f_p, p in the factor's face order
+__global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const double* __restrict__ xj,
+                                                  double* __restrict__ b) {
+  const int64_t NfW = (int64_t)a.Nf * a.W;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NfW; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = e / a.W, w = e - p * a.W;
+    double acc = 0.0;
+    for (int64_t q = __ldg(t.fj_ptr + p); q < __ldg(t.fj_ptr + p + 1); ++q) {
+      const int64_t j = __ldg(t.fj_col + q);
+      double v = xj[j * a.W + w] * __ldg(t.inv_c0 + j);
+      if (a.theta_s) v -= a.theta_s[j * a.W + w];
+      acc = fma(__ldg(t.fj_val + q), v, acc);
+    }
+    if (a.f.ptr) acc -= kTwoPi * view_at(a.f, __ldg(t.face_orig + p), w);
+    b[e] = acc;
+  }
+}
+
+// theta_next = (A^T J - x)/c0, outputs, theta_s update (time_evolution.py:562-580)
+__global__ void __launch_bounds__(256) k_update(StepArgs a, Tables t, const double* __restrict__ xj,
+                                                const double* __restrict__ J, int64_t* d_step) {
+  const int64_t NjW = (int64_t)a.Nj * a.W;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = e / a.W, w = e - j * a.W;
+    double y = 0.0;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int p = __ldg(t.jf_face + 2 * j + q);
+      if (p >= 0) y = fma(__ldg(t.jf_val + 2 * j + q), J[(int64_t)p * a.W + w], y);
+    }
+    const double th = (y - xj[e]) * __ldg(t.inv_c0 + j);
+    a.hout[e] = th;
+    if (a.th_out && a.th_slot >= 0) a.th_out[a.th_slot * NjW + e] = th;
+    if (a.I_out && a.I_slot >= 0) a.I_out[a.I_slot * NjW + e] = y + view_at(a.Is, j, w);
+    if (a.theta_s && a.Vs.ptr) a.theta_s[e] += view_at(a.Vs, j, w) * a.dt;
+  }
+  if (d_step && blockIdx.x == 0 && threadIdx.x == 0) *d_step += 1;
+}
+
+// ------------------------------------------------------------------------------------------
+// supernodal triangular solves. Work item = (supernode s, rows [r0, r1), problems [w0, w0+WB)).
+// Lane l handles problem w0 + l % WB and rows r0 + l / WB + t * (32 / WB), t < kRowsPerLane.
+// ------------------------------------------------------------------------------------------
+struct FactorDev {
+  const int32_t* col0;
+  const int32_t* k;
+  const int32_t* m;
+  const int64_t* rowptr;
+  const int32_t* rows;
+  const int64_t* valptr;
+  const double* fcol;   // F_s column-major ((k+m) x k)
+  const double* frow;   // F_s row-major
+};
+
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, const int4* __restrict__ items,
+                                                                   int n_items, int W, int WB,
+                                                                   double* __restrict__ b, double* __restrict__ z) {
+  const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  if (it >= n_items) return;
+  const int lane = threadIdx.x & 31;
+  const int4 item = items[it];
+  const int s = item.x, r0 = item.y, r1 = item.z, w0 = item.w;
+  const int LG = 32 / WB;
+  const int w = w0 + lane % WB;
+  if (w >= W) return;
+  const int rl = lane / WB;
+  const int c0 = __ldg(F.col0 + s), k = __ldg(F.k + s), m = __ldg(F.m + s), nf = k + m;
+  const double* Fs = F.fcol + __ldg(F.valptr + s);
+  double acc[kRowsPerLane];
+  int rr[kRowsPerLane];
+#pragma unroll
+  for (int t = 0; t < kRowsPerLane; ++t) {
+    acc[t] = 0.0;
+    const int r = r0 + rl + t * LG;
+    rr[t] = r < r1 ? r : r0;
+  }
+  const int jend = min(k, r1);
+  for (int j = 0; j < jend; ++j) {
+    const double bj = b[(int64_t)(c0 + j) * W + w];
+    const double* col = Fs + (int64_t)j * nf;
+#pragma unroll
+    for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(__ldg(col + rr[t]), bj, acc[t]);
+  }
+  const int32_t* R = F.rows + __ldg(F.rowptr + s);
+#pragma unroll
+  for (int t = 0; t < kRowsPerLane; ++t) {
+    const int r = r0 + rl + t * LG;
+    if (r >= r1) break;
+    if (r < k) z[(int64_t)(c0 + r) * W + w] = acc[t];
+    else atomicAdd(b + (int64_t)__ldg(R + (r - k)) * W + w, -acc[t]);
+  }
+  (void)m;
+}
+
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, const int4* __restrict__ items,
+                                                                   int n_items, int W, int WB,
+                                                                   const double* __restrict__ z, double* __restrict__ x) {
+  const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  if (it >= n_items) return;
+  const int lane = threadIdx.x & 31;
+  const int4 item = items[it];
+  const int s = item.x, i0 = item.y, i1 = item.z, w0 = item.w;
+  const int LG = 32 / WB;
+  const int w = w0 + lane % WB;
+  if (w >= W) return;
+  const int rl = lane / WB;
+  const int c0 = __ldg(F.col0 + s), k = __ldg(F.k + s), m = __ldg(F.m + s);
+  const double* Fs = F.frow + __ldg(F.valptr + s);
+  double acc[kRowsPerLane];
+  int ii[kRowsPerLane];
+#pragma unroll
+  for (int t = 0; t < kRowsPerLane; ++t) {
+    acc[t] = 0.0;
+    const int i = i0 + rl + t * LG;
+    ii[t] = i < i1 ? i : i0;
+  }
+  for (int r = i0; r < k; ++r) {
+    const double zr = z[(int64_t)(c0 + r) * W + w];
+    const double* row = Fs + (int64_t)r * k;
+#pragma unroll
+    for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(__ldg(row + ii[t]), zr, acc[t]);
+  }
+  const int32_t* R = F.rows + __ldg(F.rowptr + s);
+  for (int r = 0; r < m; ++r) {
+    const double xr = x[(int64_t)__ldg(R + r) * W + w];
+    const double* row = Fs + (int64_t)(k + r) * k;
+#pragma unroll
+    for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(-__ldg(row + ii[t]), xr, acc[t]);
+  }
+#pragma unroll
+  for (int t = 0; t < kRowsPerLane; ++t) {
+    const int i = i0 + rl + t * LG;
+    if (i >= i1) break;
+    x[(int64_t)(c0 + i) * W + w] = acc[t];
+  }
+}
+
+__global__ void k_permute_rows(const double* __restrict__ src, double* __restrict__ dst, const int32_t* __restrict__ map,
+                               int n, int W, int gather) {
+  const int64_t nW = (int64_t)n * W;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nW; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / W, w = e - i * W;
+    const int64_t o = __ldg(map + i);
+    if (gather) dst[e] = src[o * W + w];
+    else dst[o * W + w] = src[e];
+  }
+}
+
+int grid_for(int64_t n, int threads) {
+  int64_t g = (n + threads - 1) / threads;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152LL * 32));
+}
+
+template <class T>
+T* upload(const T* h, size_t n, int64_t& bytes) {
+  T* d = nullptr;
+  const size_t alloc = n ? n : 1;
+  JJA_CUDA(cudaMalloc(&d, alloc * sizeof(T)));
+  bytes += (int64_t)(alloc * sizeof(T));
+  if (h && n) JJA_CUDA(cudaMemcpy(d, h, n * sizeof(T), cudaMemcpyHostToDevice));
+  return d;
+}
+
+}  // namespace
+
+struct jja_factor {
+  std::unique_ptr<jja::Factor> f;
+};
+
+struct jja_plan {
+  int Nj = 0, Nf = 0, W = 0, width = 3, WB = 1, n_levels = 0;
+  double dt = 0.0, extrap[4] = {0, 0, 0, 0};
+  Tables t{};
+  FactorDev F{};
+  std::vector<void*> allocs;
+  std::vector<int64_t> fwd_ptr, bwd_ptr;
+  int4* fwd_items = nullptr;
+  int4* bwd_items = nullptr;
+  double *b = nullptr, *z = nullptr, *x = nullptr, *xj = nullptr;
+  int32_t* perm = nullptr;   // new -> old face
+  int64_t* d_step = nullptr;
+  int64_t bytes = 0;
+  // cached graph of a fixed-length step sequence
+  cudaGraphExec_t gexec = nullptr;
+  int g_nsteps = 0;
+  std::vector<uint64_t> g_key;
+  ~jja_plan() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    for (void* p : allocs) cudaFree(p);
+  }
+  template <class T>
+  T* up(const T* h, size_t n) {
+    T* d = upload(h, n, bytes);
+    allocs.push_back(d);
+    return d;
+  }
+};
+
+namespace {
+
+void launch_solve(jja_plan* p, cudaStream_t st) {
+  // forward: levels ascending (children before parents); b is consumed, z produced
+  for (int l = 0; l < p->n_levels; ++l) {
+    const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
+    if (!n) continue;
+    k_fwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
+        p->F, p->fwd_items + p->fwd_ptr[l], n, p->W, p->WB, p->b, p->z);
+    g_launches++;
+  }
+  // backward: levels descending; x produced
+  for (int l = p->n_levels - 1; l >= 0; --l) {
+    const int n = (int)(p->bwd_ptr[l + 1] - p->bwd_ptr[l]);
+    if (!n) continue;
+    k_bwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
+        p->F, p->bwd_items + p->bwd_ptr[l], n, p->W, p->WB, p->z, p->x);
+    g_launches++;
+  }
+}
+
+// one time step; hist rotation is done by the caller through `a`. With `ev` (6 events) the
+// stage boundaries junction | face rhs | forward | backward | update are recorded.
+void launch_step(jja_plan* p, StepArgs& a, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+  const int64_t NjW = (int64_t)p->Nj * p->W, NfW = (int64_t)p->Nf * p->W;
+  if (ev) JJA_CUDA(cudaEventRecord(ev[0], st));
+  k_junction<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj);
+  if (ev) JJA_CUDA(cudaEventRecord(ev[1], st));
+  k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(a, p->t, p->xj, p->b);
+  if (ev) JJA_CUDA(cudaEventRecord(ev[2], st));
+  g_launches += 2;
+  if (!ev) {
+    launch_solve(p, st);
+  } else {
+    // forward and backward separately so both can be timed
+    for (int l = 0; l < p->n_levels; ++l) {
+      const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
+      if (!n) continue;
+      k_fwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
+          p->F, p->fwd_items + p->fwd_ptr[l], n, p->W, p->WB, p->b, p->z);
+      g_launches++;
+    }
+    JJA_CUDA(cudaEventRecord(ev[3], st));
+    for (int l = p->n_levels - 1; l >= 0; --l) {
+      const int n = (int)(p->bwd_ptr[l + 1] - p->bwd_ptr[l]);
+      if (!n) continue;
+      k_bwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
+          p->F, p->bwd_items + p->bwd_ptr[l], n, p->W, p->WB, p->z, p->x);
+      g_launches++;
+    }
+    JJA_CUDA(cudaEventRecord(ev[4], st));
+  }
+  k_update<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj, p->x, p->d_step);
+  g_launches++;
+  if (ev) JJA_CUDA(cudaEventRecord(ev[5], st));
+}
+
+StepArgs make_args(jja_plan* p, jja_state* s) {
+  StepArgs a{};
+  a.Nj = p->Nj; a.Nf = p->Nf; a.W = p->W; a.width = p->width;
+  for (int k = 0; k < 4; ++k) { a.h[k] = s->hist[k]; a.e[k] = p->extrap[k]; }
+  a.theta_s = s->theta_s;
+  a.Is = s->Is; a.f = s->f; a.Vs = s->Vs; a.T = s->T;
+  a.noise_mode = s->noise_mode;
+  a.noise = s->noise;
+  a.seed = s->seed;
+  a.d_step = p->d_step;
+  a.th_out = s->th_out;
+  a.I_out = s->I_out;
+  a.dt = p->dt;
+  return a;
+}
+
+// rotate the history: the oldest buffer receives theta_next
+void rotate(jja_state* s, int width) {
+  const int nh = width - 1;
+  double* oldest = s->hist[nh - 1];
+  for (int k = nh - 1; k > 0; --k) s->hist[k] = s->hist[k - 1];
+  s->hist[0] = oldest;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* jja_last_error(void) { return g_err.c_str(); }
+int64_t jja_launch_count(void) { return g_launches.load(); }
+
+int jja_factor_create(int n, const int64_t* colptr, const int32_t* rowind, const double* val, const double* cx,
+                      const double* cy, const int32_t* perm, const jja_factor_opts* opts, jja_factor** out) {
+  return guarded([&] {
+    if (!out || !colptr || !rowind || !val || n <= 0) throw Error(JJA_ERR_ARG, "jja_factor_create: bad arguments");
+    jja::FactorOptions o;
+    if (opts) {
+      if (opts->nd_leaf > 0) o.nd_leaf = opts->nd_leaf;
+      o.max_supernode = opts->max_supernode;
+      o.keep_factor = opts->keep_factor;
+    }
+    std::unique_ptr<jja_factor> f(new jja_factor);
+    try {
+      f->f.reset(jja::factor_create(n, colptr, rowind, val, cx, cy, perm, o));
+    } catch (const std::runtime_error& e) {
+      const std::string msg = e.what();
+      throw Error(msg.find("positive definite") != std::string::npos ? JJA_ERR_NOT_SPD : JJA_ERR_ARG, msg);
+    }
+    *out = f.release();
+  });
+}
+
+void jja_factor_destroy(jja_factor* f) { delete f; }
+
+int jja_factor_get_stats(const jja_factor* f, jja_factor_stats* out) {
+  return guarded([&] {
+    if (!f || !out) throw Error(JJA_ERR_ARG, "null argument");
+    const jja::Factor& F = *f->f;
+    out->n = F.n;
+    out->n_supernodes = F.ns;
+    out->n_levels = F.n_levels;
+    out->max_k = F.ns ? *std::max_element(F.sn_k.begin(), F.sn_k.end()) : 0;
+    out->max_m = F.ns ? *std::max_element(F.sn_m.begin(), F.sn_m.end()) : 0;
+    out->nnz_L = F.nnz_L;
+    out->f_values = (int64_t)F.fcol.size();
+    out->factor_flops = F.factor_flops;
+  });
+}
+
+int jja_factor_get_perm(const jja_factor* f, int32_t* perm_out) {
+  return guarded([&] {
+    if (!f || !perm_out) throw Error(JJA_ERR_ARG, "null argument");
+    std::copy(f->f->perm.begin(), f->f->perm.end(), perm_out);
+  });
+}
+
+int jja_factor_solve_host(const jja_factor* f, double* b, int nrhs) {
+  return guarded([&] {
+    if (!f || !b || nrhs <= 0) throw Error(JJA_ERR_ARG, "bad arguments");
+    jja::factor_solve_host(*f->f, b, nrhs);
+  });
+}
+
+int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** out) {
+  return guarded([&] {
+    if (!d || !fac || !out) throw Error(JJA_ERR_ARG, "jja_plan_create: null argument");
+    const jja::Factor& F = *fac->f;
+    if (d->Nf != F.n) throw Error(JJA_ERR_ARG, "jja_plan_create: factor order != Nf");
+    if (d->W <= 0 || d->Nj <= 0) throw Error(JJA_ERR_ARG, "jja_plan_create: W and Nj must be positive");
+    if (d->stencil_width < 3 || d->stencil_width > 5) throw Error(JJA_ERR_ARG, "stencil width must be 3, 4 or 5");
+    std::unique_ptr<jja_plan> p(new jja_plan);
+    p->Nj = d->Nj; p->Nf = d->Nf; p->W = d->W; p->width = d->stencil_width; p->dt = d->dt;
+    for (int k = 0; k < 4; ++k) p->extrap[k] = d->extrap[k];
+    int WB = 1;
+    while (WB < std::min(d->W, 32)) WB <<= 1;
+    p->WB = WB;
+    const int Nj = d->Nj, Nf = d->Nf;
+    // face -> junction entries in the factor's face order; junction -> (<= 2) faces
+    std::vector<int64_t> fj_ptr(Nf + 1, 0);
+    std::vector<int32_t> fj_col;
+    std::vector<double> fj_val;
+    std::vector<int32_t> face_orig(Nf), jf_face(2 * (size_t)Nj, -1);
+    std::vector<double> jf_val(2 * (size_t)Nj, 0.0);
+    for (int pn = 0; pn < Nf; ++pn) {
+      const int f = F.perm[pn];
+      face_orig[pn] = f;
+      for (int64_t q = d->a_rowptr[f]; q < d->a_rowptr[f + 1]; ++q) {
+        const int j = d->a_col[q];
+        if (j < 0 || j >= Nj) throw Error(JJA_ERR_ARG, "cycle matrix column out of range");
+        fj_col.push_back(j);
+        fj_val.push_back(d->a_val[q]);
+        int slot = jf_face[2 * (size_t)j] < 0 ? 0 : (jf_face[2 * (size_t)j + 1] < 0 ? 1 : -1);
+        if (slot < 0) throw Error(JJA_ERR_ARG, "a junction lies on more than two faces (non-planar cycle matrix)");
+        jf_face[2 * (size_t)j + slot] = pn;
+        jf_val[2 * (size_t)j + slot] = d->a_val[q];
+      }
+      fj_ptr[pn + 1] = (int64_t)fj_col.size();
+    }
+    p->t.Ic = p->up(d->Ic, Nj);
+    p->t.inv_c0 = p->up(d->inv_c0, Nj);
+    p->t.coef = p->up(d->coef, (size_t)(d->stencil_width - 1) * Nj);
+    p->t.Rv = p->up(d->Rv, Nj);
+    p->t.fj_ptr = p->up(fj_ptr.data(), fj_ptr.size());
+    p->t.fj_col = p->up(fj_col.data(), fj_col.size());
+    p->t.fj_val = p->up(fj_val.data(), fj_val.size());
+    p->t.face_orig = p->up(face_orig.data(), face_orig.size());
+    p->t.jf_face = p->up(jf_face.data(), jf_face.size());
+    p->t.jf_val = p->up(jf_val.data(), jf_val.size());
+    p->perm = p->up(F.perm.data(), F.perm.size());
+    // factor blocks (column-major copy for the forward pass, row-major for the backward pass)
+    std::vector<double> frow(F.fcol.size());
+    for (int s = 0; s < F.ns; ++s) {
+      const int k = F.sn_k[s], nf = k + F.sn_m[s];
+      const double* src = F.fcol.data() + F.sn_valptr[s];
+      double* dst = frow.data() + F.sn_valptr[s];
+      for (int j = 0; j < k; ++j)
+        for (int r = 0; r < nf; ++r) dst[(int64_t)r * k + j] = src[(int64_t)j * nf + r];
+    }
+    p->F.col0 = p->up(F.sn_col0.data(), F.ns);
+    p->F.k = p->up(F.sn_k.data(), F.ns);
+    p->F.m = p->up(F.sn_m.data(), F.ns);
+    p->F.rowptr = p->up(F.sn_rowptr.data(), F.sn_rowptr.size());
+    p->F.rows = p->up(F.rows.data(), F.rows.size());
+    p->F.valptr = p->up(F.sn_valptr.data(), F.sn_valptr.size());
+    p->F.fcol = p->up(F.fcol.data(), F.fcol.size());
+    p->F.frow = p->up(frow.data(), frow.size());
+    // work items per level
+    const int LG = 32 / WB, RPI = LG * kRowsPerLane;
+    p->n_levels = F.n_levels;
+    std::vector<std::vector<int>> by_level(F.n_levels);
+    for (int s = 0; s < F.ns; ++s) by_level[F.sn_level[s]].push_back(s);
+    std::vector<int4> fi, bi;
+    p->fwd_ptr.assign(1, 0);
+    p->bwd_ptr.assign(1, 0);
+    for (int l = 0; l < F.n_levels; ++l) {
+      for (int s : by_level[l]) {
+        const int k = F.sn_k[s], nf = k + F.sn_m[s];
+        for (int r0 = 0; r0 < nf; r0 += RPI)
+          for (int w0 = 0; w0 < d->W; w0 += WB) fi.push_back(make_int4(s, r0, std::min(nf, r0 + RPI), w0));
+        for (int i0 = 0; i0 < k; i0 += RPI)
+          for (int w0 = 0; w0 < d->W; w0 += WB) bi.push_back(make_int4(s, i0, std::min(k, i0 + RPI), w0));
+      }
+      p->fwd_ptr.push_back((int64_t)fi.size());
+      p->bwd_ptr.push_back((int64_t)bi.size());
+    }
+    p->fwd_items = p->up(fi.data(), fi.size());
+    p->bwd_items = p->up(bi.data(), bi.size());
+    const size_t NfW = (size_t)Nf * d->W, NjW = (size_t)Nj * d->W;
+    p->b = p->up<double>(nullptr, NfW);
+    p->z = p->up<double>(nullptr, NfW);
+    p->x = p->up<double>(nullptr, NfW);
+    p->xj = p->up<double>(nullptr, NjW);
+    p->d_step = p->up<int64_t>(nullptr, 1);
+    JJA_CUDA(cudaMemset(p->d_step, 0, sizeof(int64_t)));
+    JJA_CUDA(cudaDeviceSynchronize());
+    *out = p.release();
+  });
+}
+
+void jja_plan_destroy(jja_plan* p) { delete p; }
+
+int64_t jja_plan_device_bytes(const jja_plan* p) { return p ? p->bytes : 0; }
+
+int jja_solve(jja_plan* p, const double* b, double* x, void* stream) {
+  return guarded([&] {
+    if (!p || !b || !x) throw Error(JJA_ERR_ARG, "jja_solve: null argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t NfW = (int64_t)p->Nf * p->W;
+    k_permute_rows<<<grid_for(NfW, 256), 256, 0, st>>>(b, p->b, p->perm, p->Nf, p->W, 1);
+    g_launches++;
+    launch_solve(p, st);
+    k_permute_rows<<<grid_for(NfW, 256), 256, 0, st>>>(p->x, x, p->perm, p->Nf, p->W, 0);
+    g_launches++;
+    JJA_CUDA(cudaGetLastError());
+  });
+}
+
+int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const int64_t* I_slot, int use_graph,
+            void* stream) {
+  return guarded([&] {
+    if (!p || !s || nsteps < 0) throw Error(JJA_ERR_ARG, "jja_run: bad arguments");
+    for (int k = 0; k < p->width - 1; ++k)
+      if (!s->hist[k]) throw Error(JJA_ERR_ARG, "jja_run: missing history buffer");
+    if (s->noise_mode == JJA_NOISE_BUFFER && !s->noise) throw Error(JJA_ERR_ARG, "jja_run: noise buffer missing");
+    cudaStream_t st = (cudaStream_t)stream;
+    JJA_CUDA(cudaMemcpyAsync(p->d_step, &s->step, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    const int period = p->width - 1;  // history rotation period
+    int i = 0;
+    while (i < nsteps) {
+      // a run of steps that store nothing can be replayed from a captured graph
+      int run = 0;
+      while (i + run < nsteps && (!th_slot || th_slot[i + run] < 0) && (!I_slot || I_slot[i + run] < 0)) ++run;
+      const int G = 16 * period;
+      // capture needs a non-default stream; the per-step noise buffer is refilled by the host
+      if (use_graph && st != nullptr && run >= G && s->noise_mode != JJA_NOISE_BUFFER) {
+        std::vector<uint64_t> key = {(uint64_t)s->hist[0], (uint64_t)s->hist[1], (uint64_t)s->hist[2],
+                                     (uint64_t)s->hist[3], (uint64_t)s->theta_s, (uint64_t)s->Is.ptr,
+                                     (uint64_t)s->f.ptr, (uint64_t)s->Vs.ptr, (uint64_t)s->T.ptr,
+                                     (uint64_t)s->noise_mode, s->seed, (uint64_t)stream,
+                                     (uint64_t)s->Is.stride_n, (uint64_t)s->Is.stride_w,
+                                     (uint64_t)s->f.stride_n, (uint64_t)s->f.stride_w,
+                                     (uint64_t)s->T.stride_n, (uint64_t)s->T.stride_w,
+                                     (uint64_t)s->Vs.stride_n, (uint64_t)s->Vs.stride_w};
+        if (!p->gexec || p->g_key != key) {
+          if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
+          cudaGraph_t g;
+          jja_state tmp = *s;
+          JJA_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+          for (int q = 0; q < G; ++q) {
+            StepArgs a = make_args(p, &tmp);
+            a.hout = tmp.hist[period - 1];
+            a.th_slot = a.I_slot = -1;
+            launch_step(p, a, st);
+            rotate(&tmp, p->width);
+          }
+          JJA_CUDA(cudaStreamEndCapture(st, &g));
+          JJA_CUDA(cudaGraphInstantiate(&p->gexec, g, 0));
+          cudaGraphDestroy(g);
+          p->g_key = key;
+        }
+        const int reps = run / G;
+        for (int r = 0; r < reps; ++r) JJA_CUDA(cudaGraphLaunch(p->gexec, st));
+        i += reps * G;  // G is a multiple of the rotation period: pointers are unchanged
+        run -= reps * G;
+      }
+      const int eager = (i < nsteps) ? std::max(run, 1) : 0;
+      for (int q = 0; q < eager && i < nsteps; ++q, ++i) {
+        StepArgs a = make_args(p, s);
+        a.hout = s->hist[period - 1];
+        a.th_slot = th_slot ? th_slot[i] : -1;
+        a.I_slot = I_slot ? I_slot[i] : -1;
+        launch_step(p, a, st);
+        rotate(s, p->width);
+      }
+    }
+    JJA_CUDA(cudaGetLastError());
+    s->step += nsteps;
+  });
+}
+
+int jja_run_timed(jja_plan* p, jja_state* s, int nsteps, double* stage_ms, void* stream) {
+  return guarded([&] {
+    if (!p || !s || nsteps <= 0 || !stage_ms) throw Error(JJA_ERR_ARG, "jja_run_timed: bad arguments");
+    if (s->noise_mode == JJA_NOISE_BUFFER) throw Error(JJA_ERR_ARG, "jja_run_timed: host noise buffer not supported");
+    cudaStream_t st = (cudaStream_t)stream;
+    JJA_CUDA(cudaMemcpyAsync(p->d_step, &s->step, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    std::vector<cudaEvent_t> ev(6 * (size_t)nsteps);
+    for (auto& e : ev) JJA_CUDA(cudaEventCreate(&e));
+    const int period = p->width - 1;
+    for (int i = 0; i < nsteps; ++i) {
+      StepArgs a = make_args(p, s);
+      a.hout = s->hist[period - 1];
+      a.th_slot = a.I_slot = -1;
+      launch_step(p, a, st, ev.data() + 6 * (size_t)i);
+      rotate(s, p->width);
+    }
+    JJA_CUDA(cudaEventSynchronize(ev.back()));
+    for (int k = 0; k < 6; ++k) stage_ms[k] = 0.0;
+    for (int i = 0; i < nsteps; ++i) {
+      const cudaEvent_t* e = ev.data() + 6 * (size_t)i;
+      for (int k = 0; k < 5; ++k) {
+        float ms = 0.f;
+        JJA_CUDA(cudaEventElapsedTime(&ms, e[k], e[k + 1]));
+        stage_ms[k] += ms;
+      }
+    }
+    float total = 0.f;
+    JJA_CUDA(cudaEventElapsedTime(&total, ev.front(), ev.back()));
+    stage_ms[5] = total;
+    for (auto& e : ev) cudaEventDestroy(e);
+    s->step += nsteps;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,182 @@
+"""Host-side plan: the face-space matrix, its factor and the device plan, cached.
+
+The reference rebuilds and refactorises K = A (L + diag(1/Cnext)) A^T inside every
+time_evolution_core call (time_evolution.py:504-506). Here the factor (host, FP64,
+nested dissection + supernodal Cholesky in libjja_gb300) and the device plan (factor
+blocks + circuit tables uploaded once) are cached by the content that determines them:
+the cycle matrix, R, C, L, dt and the stencil width (and W for the device plan), so
+repeated compute() calls on the same circuit (e.g. an annealing schedule or a sweep)
+pay the factorisation once.
+"""
+import ctypes
+import hashlib
+from collections import OrderedDict
+
+import numpy as np
+import scipy.sparse
+
+from . import _native as N
+
+_FACTORS = OrderedDict()
+_PLANS = OrderedDict()
+MAX_FACTORS = 4
+MAX_PLANS = 4
+
+# Extrapolation weights of the CPR argument on theta(t-1), theta(t-2), ... (time_evolution.py:547-553)
+EXTRAP = {3: (2.0, -1.0), 4: (3.0, -3.0, 1.0), 5: (4.0, -6.0, 4.0, -1.0)}
+
+
+def _digest(*arrays):
+    h = hashlib.blake2b(digest_size=16)
+    for a in arrays:
+        a = np.ascontiguousarray(a)
+        h.update(str(a.dtype).encode() + str(a.shape).encode())
+        h.update(a.view(np.uint8).ravel() if a.size else b"")
+    return h.hexdigest()
+
+
+def coefficients(circuit, dt, stencil):
+    """Per-junction stencil coefficients (time_evolution.py:472-478, 489, 495, 501)."""
+    s1, s2 = stencil
+    Rv = 1.0 / (dt * np.asarray(circuit._R(), np.float64))
+    Cv = np.asarray(circuit._C(), np.float64) / dt ** 2
+    coef = [s1[k] * Rv + s2[k] * Cv for k in range(len(s1))]
+    return Rv, Cv, coef
+
+
+def face_matrix(circuit, dt):
+    """K = A (L + diag(1/(Cv + Rv))) A^T as CSC with sorted indices (time_evolution.py:504-505)."""
+    A = scipy.sparse.csc_matrix(circuit.get_cycle_matrix()).astype(np.float64)
+    Rv = 1.0 / (dt * np.asarray(circuit._R(), np.float64))
+    Cv = np.asarray(circuit._C(), np.float64) / dt ** 2
+    L = circuit._L()
+    L = scipy.sparse.csc_matrix(L) if not scipy.sparse.issparse(L) else L
+    K = (A @ (L + scipy.sparse.diags(1.0 / (Cv + Rv), 0)) @ A.T).tocsc()
+    K.sum_duplicates()
+    K.sort_indices()
+    return A, K
+
+
+class HostFactor:
+    """Ordered supernodal Cholesky of K (owned C object)."""
+
+    def __init__(self, K, coords=None, perm=None, nd_leaf=8, max_supernode=0, keep_factor=False):
+        L = N.lib()
+        n = K.shape[0]
+        self.n = n
+        colptr = np.ascontiguousarray(K.indptr, np.int64)
+        rowind = np.ascontiguousarray(K.indices, np.int32)
+        val = np.ascontiguousarray(K.data, np.float64)
+        cx = cy = None
+        if coords is not None:
+            cx = np.ascontiguousarray(coords[0], np.float64)
+            cy = np.ascontiguousarray(coords[1], np.float64)
+        pm = None if perm is None else np.ascontiguousarray(perm, np.int32)
+        opts = N.FactorOpts(nd_leaf, max_supernode, int(keep_factor))
+        h = ctypes.c_void_p()
+        N.check(L.jja_factor_create(n, N.ptr(colptr, ctypes.c_int64), N.ptr(rowind, ctypes.c_int32), N.ptr(val),
+                                    N.ptr(cx), N.ptr(cy), N.ptr(pm, ctypes.c_int32), ctypes.byref(opts),
+                                    ctypes.byref(h)))
+        self.handle = h
+        st = N.FactorStats()
+        N.check(L.jja_factor_get_stats(h, ctypes.byref(st)))
+        self.stats = {k: getattr(st, k) for k, _ in N.FactorStats._fields_}
+
+    def perm(self):
+        out = np.empty(self.n, np.int32)
+        N.check(N.lib().jja_factor_get_perm(self.handle, N.ptr(out, ctypes.c_int32)))
+        return out
+
+    def solve_host(self, b):
+        """Host solve (diagnostic). b: (n,) or (n, nrhs)."""
+        b = np.array(b, dtype=np.float64, order="C", copy=True)
+        nrhs = 1 if b.ndim == 1 else b.shape[1]
+        N.check(N.lib().jja_factor_solve_host(self.handle, N.ptr(b), nrhs))
+        return b
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and N._lib is not None:
+            N._lib.jja_factor_destroy(h)
+            self.handle = None
+
+
+class DevicePlan:
+    """Circuit tables + factor uploaded for W problems (owned C object)."""
+
+    def __init__(self, circuit, factor, A, W, dt, stencil_width, stencil):
+        Nj, Nf = circuit._Nj(), circuit._Nf()
+        Rv, Cv, coef = coefficients(circuit, dt, stencil)
+        Acsr = scipy.sparse.csr_matrix(A)
+        Acsr.sort_indices()
+        self._keep = dict(
+            rowptr=np.ascontiguousarray(Acsr.indptr, np.int64),
+            col=np.ascontiguousarray(Acsr.indices, np.int32),
+            val=np.ascontiguousarray(Acsr.data, np.float64),
+            Ic=np.ascontiguousarray(circuit._Ic(), np.float64),
+            inv_c0=np.ascontiguousarray(1.0 / coef[0], np.float64),
+            coef=np.ascontiguousarray(np.stack(coef[1:]), np.float64),
+            Rv=np.ascontiguousarray(Rv, np.float64))
+        k = self._keep
+        ex = (ctypes.c_double * 4)(*(list(EXTRAP[stencil_width]) + [0.0] * (4 - len(EXTRAP[stencil_width]))))
+        d = N.PlanDesc(Nj, Nf, W, stencil_width, N.ptr(k["rowptr"], ctypes.c_int64), N.ptr(k["col"], ctypes.c_int32),
+                       N.ptr(k["val"]), N.ptr(k["Ic"]), N.ptr(k["inv_c0"]), N.ptr(k["coef"]), N.ptr(k["Rv"]), ex, dt)
+        h = ctypes.c_void_p()
+        N.check(N.lib().jja_plan_create(ctypes.byref(d), factor.handle, ctypes.byref(h)))
+        self.handle = h
+        self.Nj, self.Nf, self.W = Nj, Nf, W
+        self.inv_c0 = k["inv_c0"]
+        self.device_bytes = N.lib().jja_plan_device_bytes(h)
+
+    def solve(self, b_dev, x_dev, stream=0):
+        N.check(N.lib().jja_solve(self.handle, ctypes.c_void_p(b_dev), ctypes.c_void_p(x_dev), ctypes.c_void_p(stream)))
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and N._lib is not None:
+            N._lib.jja_plan_destroy(h)
+            self.handle = None
+
+
+def _coords(circuit):
+    try:
+        cx, cy = circuit.get_face_centroids()
+        return np.asarray(cx, np.float64), np.asarray(cy, np.float64)
+    except Exception:
+        return None
+
+
+def get_factor(circuit, dt, nd_leaf=8):
+    A, K = face_matrix(circuit, dt)
+    key = (_digest(K.indptr, K.indices, K.data), nd_leaf)
+    f = _FACTORS.get(key)
+    if f is None:
+        f = HostFactor(K, coords=_coords(circuit), nd_leaf=nd_leaf)
+        _FACTORS[key] = (f, A)
+        while len(_FACTORS) > MAX_FACTORS:
+            _FACTORS.popitem(last=False)
+    else:
+        _FACTORS.move_to_end(key)
+        f = f[0]
+    return _FACTORS[key][0], A, key
+
+
+def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=8):
+    factor, A, fkey = get_factor(circuit, dt, nd_leaf)
+    Rv, Cv, coef = coefficients(circuit, dt, stencil)
+    key = (fkey, W, stencil_width, _digest(np.asarray(circuit._Ic(), np.float64), *coef, Rv,
+                                            A.indptr, A.indices, A.data))
+    p = _PLANS.get(key)
+    if p is None:
+        p = DevicePlan(circuit, factor, A, W, dt, stencil_width, stencil)
+        _PLANS[key] = p
+        while len(_PLANS) > MAX_PLANS:
+            _PLANS.popitem(last=False)
+    else:
+        _PLANS.move_to_end(key)
+    return p
+
+
+def clear_cache():
+    _PLANS.clear()
+    _FACTORS.clear()

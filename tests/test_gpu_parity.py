@@ -1,0 +1,127 @@
+"""GPU parity: the CUDA path against the reference's golden vectors and the CPU oracle.
+
+Tolerances (FP64 on both sides, different summation orders in the face-space solve):
+* T = 0 trajectories: |theta_gpu - theta_ref| <= 1e-9 * max(1, |theta_ref|), the bar the
+  reference comparison is held to over a 2000-step run;
+* noisy runs with the reference's own noise draws replayed (noise="numpy"): same bar;
+* the face-space solve alone: relative 1e-11 against scipy's sparse direct solve.
+"""
+import numpy as np
+import pytest
+import scipy.sparse.linalg
+
+import golden_cases as gc
+from oracle import rcsj_oracle
+from pyjjasim_gb300 import TimeEvolutionProblem, backend
+from pyjjasim_gb300 import plan as P
+from pyjjasim_gb300.circuit import HoneycombArray, SquareArray, TriangularArray
+
+pytestmark = pytest.mark.gpu
+TRAJ_RTOL = 1e-9
+
+
+def close(actual, desired, rtol=TRAJ_RTOL):
+    scale = max(1.0, float(np.abs(desired).max()))
+    err = float(np.abs(actual - desired).max())
+    assert err <= rtol * scale, f"max abs err {err:.3e} > {rtol:.1e} * {scale:.3e}"
+
+
+@pytest.mark.parametrize("name", gc.case_names())
+def test_golden_parity(name):
+    z = gc.load(name)
+    prob = gc.problem(z)
+    s = gc.seed(z)
+    if s is not None:
+        np.random.seed(s)
+    res = prob.compute(noise="numpy")
+    close(res.get_theta(), z["theta"])
+    close(res.get_current(), z["current"])
+    close(res.get_voltage(), z["voltage"], rtol=1e-8)
+    assert np.array_equal(res.get_vortex_configuration(), z["vortex"])
+
+
+@pytest.mark.parametrize("make,W", [(lambda: SquareArray(9, 13), 1), (lambda: SquareArray(20, 20), 37),
+                                    (lambda: HoneycombArray(6, 5), 64), (lambda: TriangularArray(7, 6), 3),
+                                    (lambda: SquareArray(64, 64), 40)])
+def test_face_solve_matches_scipy(make, W):
+    c = make()
+    c.set_inductance(0.05)
+    dt = 0.05
+    A, K = P.face_matrix(c, dt)
+    b = np.random.default_rng(W).standard_normal((K.shape[0], W))
+    x = backend.solve_faces(c, dt, b)
+    ref = scipy.sparse.linalg.spsolve(K.tocsc(), b).reshape(x.shape)
+    close(x, ref, rtol=1e-11)
+
+
+def _mixed_problem(c, W, Nt, seed):
+    rng = np.random.default_rng(seed)
+    Nj, Nf = c.junction_count(), c.face_count()
+    Is = c.current_base(0.3)[:, None, None] * np.linspace(0.2, 1.4, W)[None, :, None]
+    f = rng.uniform(0, 0.5, (Nf, 1, 1))
+    th1 = rng.standard_normal((Nj, W)) * 0.3
+    return TimeEvolutionProblem(c, time_step=0.07, time_step_count=Nt, current_sources=Is, external_flux=f,
+                                config_at_minus_1=th1, config_at_minus_2=th1 * 0.98,
+                                store_time_steps=np.arange(0, Nt, 7))
+
+
+@pytest.mark.parametrize("make,W", [(lambda: HoneycombArray(5, 6), 5), (lambda: TriangularArray(6, 5), 7),
+                                    (lambda: SquareArray(11, 17), 33)])
+def test_against_oracle(make, W):
+    c = make()
+    c.set_capacitance(0.3)
+    c.set_inductance(0.2)
+    prob = _mixed_problem(c, W, 300, W)
+    th_o, I_o, V_o = rcsj_oracle.time_evolution(prob)
+    res = prob.compute()
+    close(res.get_theta(), th_o)
+    close(res.get_current(), I_o)
+    close(res.get_voltage(), V_o, rtol=1e-8)
+
+
+def test_graph_and_eager_paths_agree():
+    c = SquareArray(24, 24)
+    W = 16
+    Is = c.current_base(0.0)[:, None, None] * np.linspace(0, 2, W)[None, :, None]
+    prob = TimeEvolutionProblem(c, time_step=0.05, time_step_count=400, current_sources=Is, external_flux=0.25,
+                                store_time_steps=[399])
+    th_g, _ = backend.time_evolution_core(prob, prob.store_time_steps, prob.store_time_steps, use_graph=True)
+    th_e, _ = backend.time_evolution_core(prob, prob.store_time_steps, prob.store_time_steps, use_graph=False)
+    close(th_g, th_e, rtol=1e-11)
+
+
+def test_full_size_kirchhoff_invariants():
+    """IV-sweep shape at full size (128x128 array, W=512): A theta + 2 pi f = 0 (no inductance)
+    and current conservation M (I - Is) = 0 after many steps; both are size-independent."""
+    c = SquareArray(128, 128)
+    W, Nt, f = 512, 200, 0.25
+    Is = c.current_base(0.0)[:, None, None] * np.linspace(0, 2, W)[None, :, None]
+    prob = TimeEvolutionProblem(c, time_step=0.05, time_step_count=Nt, current_sources=Is, external_flux=f,
+                                store_time_steps=[Nt - 1], store_voltage=False)
+    res = prob.compute()
+    th = res.get_theta()[:, :, 0]
+    I = res.get_current()[:, :, 0]
+    A, M = c.get_cycle_matrix(), c.get_cut_matrix()
+    kvl = A @ th + 2 * np.pi * f
+    assert np.abs(kvl).max() < 1e-9 * max(1.0, np.abs(th).max())
+    kcl = M @ (I - Is[:, :, 0])
+    assert np.abs(kcl).max() < 1e-9
+    assert np.all(np.isfinite(th))
+
+
+def test_philox_noise_statistics():
+    """On-device noise: mean-square junction voltage at T>0, C=0, Is=0 follows the
+    fluctuation amplitude; checked against the oracle driven by its own normal draws."""
+    c = SquareArray(16, 16)
+    W, Nt, T = 64, 400, 0.05
+    prob = TimeEvolutionProblem(c, time_step=0.05, time_step_count=Nt, temperature=T * np.ones((1, W, 1)),
+                                store_time_steps=np.arange(Nt // 2, Nt), store_current=False)
+    res = prob.compute(noise="philox", seed=1234)
+    V = res.get_voltage()
+    rng = np.random.default_rng(0)
+    th_o, _, V_o = rcsj_oracle.time_evolution(prob, noise=lambda i: rng.standard_normal((c.junction_count(), W)))
+    ms_gpu, ms_cpu = float(np.mean(V ** 2)), float(np.mean(V_o ** 2))
+    assert abs(ms_gpu - ms_cpu) < 0.03 * ms_cpu
+    # different seeds give different paths, the same seed the same path
+    res2 = prob.compute(noise="philox", seed=1234)
+    close(res2.get_theta(), res.get_theta(), rtol=1e-10)
