@@ -204,6 +204,29 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def profile_mode(args):
+    """Minimal launch sequence for ncu: every kernel launch of a step is issued eagerly.
+
+    Launch order per step: k_junction, k_face_rhs, k_fwd_level x n_levels (leaves first),
+    k_bwd_level x n_levels (root first), k_update."""
+    import torch
+    import pyjjasim_gb300 as G
+    from pyjjasim_gb300.backend import GpuSimulation
+    torch.cuda.set_device(0)
+    prob = make_problem(G, 1, np.linspace(0.0, 2.0, args.W))
+    sim = GpuSimulation(prob)
+    sim.run(3, use_graph=False)
+    sim.synchronize()
+    t0 = time.perf_counter()
+    sim.run(args.profile_steps, use_graph=False)
+    sim.synchronize()
+    dt = time.perf_counter() - t0
+    ok = bool(torch.isfinite(sim.theta()).all())
+    print(json.dumps({"profile_steps": args.profile_steps, "W": args.W, "seconds": dt, "finite": ok}))
+    if not ok:
+        sys.exit(1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -212,10 +235,15 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="profiling mode: plan, 3 eager warm-up steps, then this many eager steps, nothing else")
+    ap.add_argument("--W", type=int, default=W_BATCH, help="problems per launch (profiling mode)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_steps:
+        return profile_mode(args)
 
     import torch
     import torch.distributed as dist

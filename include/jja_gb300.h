@@ -40,6 +40,9 @@ typedef struct {
   int nd_leaf;        /* nested-dissection leaf size (<= 0: default 8) */
   int max_supernode;  /* cap on supernode width (0: none) */
   int keep_factor;    /* keep plain Cholesky columns for host checks */
+  int relax_zeros;    /* merge a child supernode into its parent if that adds <= this many zeros */
+  double relax_frac;  /* ... or <= this fraction of the merged block (both 0: fundamental only;
+                         negative values select the defaults 64 and 0.1) */
 } jja_factor_opts;
 
 typedef struct {
@@ -65,6 +68,10 @@ void jja_factor_destroy(jja_factor* f);
 int jja_factor_get_stats(const jja_factor* f, jja_factor_stats* out);
 /* perm_out[n]: new -> old face order used by the factor (a postordered nested dissection). */
 int jja_factor_get_perm(const jja_factor* f, int32_t* perm_out);
+/* Supernode table (arrays of n_supernodes entries, any may be NULL): first column, width k,
+ * off-diagonal row count m, elimination-tree level (leaves 0) and parent (-1 at roots). */
+int jja_factor_get_supernodes(const jja_factor* f, int32_t* col0, int32_t* k, int32_t* m, int32_t* level,
+                              int32_t* parent);
 /* Host solve K x = b in place (b: n x nrhs row-major, original order). Diagnostic only:
  * used to check a factor without a GPU; the time-stepping path solves on the GPU. */
 int jja_factor_solve_host(const jja_factor* f, double* b, int nrhs);
@@ -136,6 +143,11 @@ int jja_run_timed(jja_plan* p, jja_state* st, int nsteps, double* stage_ms, void
 /* Face-space solve on the device: x = K^{-1} b for W right-hand sides (device arrays
  * Nf x W, original face order). Exposed for tests of the triangular-solve kernels. */
 int jja_solve(jja_plan* p, const double* b, double* x, void* stream);
+
+/* out[i] = sin(x[i]) with the library's device sine (device arrays of n doubles), the one
+ * the junction-current kernels use for Ic sin(theta) (pyjjasim static_problem.py:82-85).
+ * Exposed so tests can bound its error against a correctly rounded sine. */
+int jja_eval_sin(jja_plan* p, const double* x, double* out, int64_t n, void* stream);
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* jja_last_error(void);

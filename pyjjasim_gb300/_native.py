@@ -19,7 +19,8 @@ NOISE_NONE, NOISE_BUFFER, NOISE_PHILOX = 0, 1, 2
 
 
 class FactorOpts(ctypes.Structure):
-    _fields_ = [("nd_leaf", c_int), ("max_supernode", c_int), ("keep_factor", c_int)]
+    _fields_ = [("nd_leaf", c_int), ("max_supernode", c_int), ("keep_factor", c_int), ("relax_zeros", c_int),
+                ("relax_frac", c_double)]
 
 
 class FactorStats(ctypes.Structure):
@@ -51,6 +52,7 @@ SIGNATURES = {
     "jja_factor_destroy": (None, [c_void_p]),
     "jja_factor_get_stats": (c_int, [c_void_p, ctypes.POINTER(FactorStats)]),
     "jja_factor_get_perm": (c_int, [c_void_p, P_i32]),
+    "jja_factor_get_supernodes": (c_int, [c_void_p, P_i32, P_i32, P_i32, P_i32, P_i32]),
     "jja_factor_solve_host": (c_int, [c_void_p, P_f64, c_int]),
     "jja_plan_create": (c_int, [ctypes.POINTER(PlanDesc), c_void_p, ctypes.POINTER(c_void_p)]),
     "jja_plan_destroy": (None, [c_void_p]),
@@ -58,6 +60,7 @@ SIGNATURES = {
     "jja_run": (c_int, [c_void_p, ctypes.POINTER(State), c_int, P_i64, P_i64, c_int, c_void_p]),
     "jja_run_timed": (c_int, [c_void_p, ctypes.POINTER(State), c_int, P_f64, c_void_p]),
     "jja_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "jja_eval_sin": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
     "jja_last_error": (ctypes.c_char_p, []),
     "jja_launch_count": (c_int64, []),
 }

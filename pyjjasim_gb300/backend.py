@@ -191,7 +191,8 @@ class GpuSimulation:
         ms = np.zeros(6)
         N.check(N.lib().jja_run_timed(self.plan.handle, ctypes.byref(self.state), int(nsteps), N.ptr(ms),
                                       ctypes.c_void_p(self.stream.cuda_stream)))
-        return dict(zip(("junction", "face_rhs", "forward", "backward", "update", "total"), ms.tolist()))
+        return dict(zip(("first_junction", "face_rhs", "forward", "backward", "update_junction", "total"),
+                        ms.tolist()))
 
     def theta_ptr(self):
         return self.state.hist[0]

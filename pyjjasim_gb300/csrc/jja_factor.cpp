@@ -384,6 +384,50 @@ Factor* factor_create(int n, const int64_t* colptr, const int32_t* rowind, const
     if (!merge) sstart.push_back(j);
   }
   sstart.push_back(n);
+  // relaxed amalgamation: merge a supernode into its parent when its columns directly
+  // precede the parent's and the merge adds few explicit zeros. A child's structure is
+  // contained in the parent's columns plus the parent's structure, so the merged block
+  // has the parent's off-diagonal rows; the child's columns gain k_c (k_p + m_p - m_c)
+  // zero entries. Chains of single-column supernodes (a separator face touching one more
+  // ancestor face than its neighbours) collapse, which shortens the level schedule.
+  if (opt.relax_zeros > 0 || opt.relax_frac > 0.0) {
+    const int nf0 = (int)sstart.size() - 1;
+    std::vector<int> c2s(n);
+    for (int s = 0; s < nf0; ++s)
+      for (int j = sstart[s]; j < sstart[s + 1]; ++j) c2s[j] = s;
+    std::vector<int> a(nf0), b(nf0), par(nf0, -1), alive(nf0, 1), rep(nf0);
+    std::vector<int64_t> msz(nf0);
+    for (int s = 0; s < nf0; ++s) {
+      a[s] = sstart[s];
+      b[s] = sstart[s + 1];
+      msz[s] = cc[b[s] - 1];
+      rep[s] = s;
+      if (parent[b[s] - 1] >= 0) par[s] = c2s[parent[b[s] - 1]];
+    }
+    auto find = [&](int x) {
+      while (rep[x] != x) { rep[x] = rep[rep[x]]; x = rep[x]; }
+      return x;
+    };
+    for (int s = 0; s < nf0; ++s) {  // postorder: children before parents
+      if (par[s] < 0) continue;
+      const int p = find(par[s]);
+      if (b[s] != a[p]) continue;
+      const int64_t kc = b[s] - a[s], kp = b[p] - a[p], mp = msz[p], mc = msz[s];
+      const int64_t extra = kc * (kp + mp - mc);
+      const int64_t km = kc + kp;
+      const double merged = (double)km * (km + 1) / 2.0 + (double)km * mp;
+      if (opt.max_supernode > 0 && km > opt.max_supernode) continue;
+      if (extra > opt.relax_zeros && extra > opt.relax_frac * merged) continue;
+      a[p] = a[s];
+      alive[s] = 0;
+      rep[s] = p;
+    }
+    std::vector<int> ns2;
+    for (int s = 0; s < nf0; ++s)
+      if (alive[s]) ns2.push_back(a[s]);
+    ns2.push_back(n);
+    sstart.swap(ns2);
+  }
   const int ns = (int)sstart.size() - 1;
   std::vector<int> col2sn(n);
   for (int s = 0; s < ns; ++s)

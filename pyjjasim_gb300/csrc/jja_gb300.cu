@@ -55,6 +55,7 @@ int guarded(F&& f) {
 
 constexpr int kWarpsPerBlock = 4;   // level kernels: one warp per work item
 constexpr int kRowsPerLane = 4;     // rows of a work item handled by one lane
+constexpr int kUnroll = 4;          // columns whose loads are issued ahead of their FMAs
 constexpr double kTwoPi = 6.283185307179586;
 
 // ------------------------------------------------------------------------------------------
@@ -98,7 +99,7 @@ struct StepArgs {
   int noise_mode;
   const double* noise;
   uint64_t seed;
-  const int64_t* d_step;
+  int64_t* d_step;
   int64_t th_slot, I_slot;
   double* th_out;
   double* I_out;
@@ -117,70 +118,128 @@ struct Tables {
   const int32_t* face_orig;
   const int32_t* jf_face;  // 2 per junction (permuted face or -1)
   const double* jf_val;
+  const double2* sincos;   // {sin, cos}(k pi / 2048), k < 4096
 };
 
-// x(j, w) for this step (time_evolution.py:533-558)
-__global__ void __launch_bounds__(256) k_junction(StepArgs a, Tables t, double* __restrict__ xj) {
+// ------------------------------------------------------------------------------------------
+// sin(x) in FP64 with few FP64 instructions (GB300's FP64 pipe is ~60x narrower than FP32).
+// Cody-Waite reduction x = k pi/2048 + t, |t| <= pi/4096, with pi/2048 = C1 + C2 + C3 where C1
+// and C2 carry 26 bits each (k C1 and k C2 are exact for |k| < 2^27); then
+//   sin(x) = S + C t - S t^2/2 - C t^3/6 + S t^4/24 + O(t^5),  S, C = sin, cos(k pi/2048),
+// from a 4096-entry table computed on the host in extended precision. |t^3/6| < 7.6e-11 and
+// |t^4/24| < 1.5e-14, so those two terms are evaluated in FP32 (absolute error < 2e-17);
+// the rest is three FP64 FMAs. The O(t^5) remainder is below 3e-18. |x| >= 2e5 (or NaN)
+// falls back to the CUDA math library.
+// ------------------------------------------------------------------------------------------
+constexpr double kSinScale = 0x1.45f306dc9c883p+9;   // 2048 / pi
+constexpr double kSinC1 = 0x1.921fb58000000p-10;
+constexpr double kSinC2 = -0x1.dde9740000000p-37;
+constexpr double kSinC3 = 0x1.1a62633145c07p-64;
+constexpr double kRoundMagic = 6755399441055744.0;   // 1.5 * 2^52: adding it rounds to an integer
+constexpr int kSinTable = 4096;
+
+__device__ __forceinline__ double fast_sin(double x, const double2* __restrict__ tab) {
+  if (!(fabs(x) < 2.0e5)) return sin(x);
+  const double s = fma(x, kSinScale, kRoundMagic);
+  const int k = __double2loint(s);
+  const double kd = s - kRoundMagic;
+  double t = fma(-kd, kSinC1, x);
+  t = fma(-kd, kSinC2, t);
+  t = fma(-kd, kSinC3, t);
+  const double2 sc = __ldg(tab + (k & (kSinTable - 1)));
+  const double mh = (-0.5 * t) * t;          // -t^2/2
+  double r = fma(sc.y, t, sc.x);             // S + C t
+  r = fma(sc.x, mh, r);                      // - S t^2/2
+  const float tf = __double2float_rn(t);
+  const float t2 = tf * tf;
+  const float tail = fmaf(__double2float_rn(sc.x) * (1.0f / 24.0f), t2 * t2,
+                          -(__double2float_rn(sc.y) * (1.0f / 6.0f)) * (t2 * tf));
+  return r + (double)tail;
+}
+
+// q(j, w) = x / c0 for the step whose phase history is th[0..] (time_evolution.py:533-558):
+//   x = sqrt(2 T Rv) xi - Is + Ic sin(sum_k e_k th_k) + sum_k c_k th_k
+__device__ __forceinline__ double junction_q(const StepArgs& a, const Tables& t, int64_t e, int64_t j, int64_t w,
+                                            const double* th, const jja_view& Is, int64_t step) {
+  double arg = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (k < a.width - 1) arg = fma(a.e[k], th[k], arg);
+  double X = __ldg(t.Ic + j) * fast_sin(arg, t.sincos);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (k < a.width - 1) X = fma(__ldg(t.coef + (int64_t)k * a.Nj + j), th[k], X);
+  double fl = 0.0;
+  if (a.noise_mode != JJA_NOISE_NONE) {
+    const double T = view_at(a.T, j, w);
+    const double xi = a.noise_mode == JJA_NOISE_BUFFER ? a.noise[e] : philox_normal(a.seed, (uint64_t)e, (uint64_t)step);
+    fl = sqrt(2.0 * T * __ldg(t.Rv + j)) * xi;
+  }
+  return ((fl - view_at(Is, j, w)) + X) * __ldg(t.inv_c0 + j);
+}
+
+// q for the first step of a run, from the stored phase history
+__global__ void __launch_bounds__(256) k_junction(StepArgs a, Tables t, double* __restrict__ q) {
   const int64_t NjW = (int64_t)a.Nj * a.W;
-  const int64_t step = a.d_step ? *a.d_step : 0;
+  const int64_t step = *a.d_step;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = e / a.W, w = e - j * a.W;
-    double arg = 0.0, X;
     double th[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-      if (k < a.width - 1) { th[k] = a.h[k][e]; arg = fma(a.e[k], th[k], arg); }
-    X = __ldg(t.Ic + j) * sin(arg);
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      if (k < a.width - 1) X = fma(__ldg(t.coef + (int64_t)k * a.Nj + j), th[k], X);
-    double fl = 0.0;
-    if (a.noise_mode != JJA_NOISE_NONE) {
-      const double T = view_at(a.T, j, w);
-      const double xi = a.noise_mode == JJA_NOISE_BUFFER ? a.noise[e] : philox_normal(a.seed, (uint64_t)e, (uint64_t)step);
-      fl = sqrt(2.0 * T * __ldg(t.Rv + j)) * xi;
-    }
-    xj[e] = (fl - view_at(a.Is, j, w)) + X;
+    for (int k = 0; k < 4; ++k) th[k] = (k < a.width - 1) ? a.h[k][e] : 0.0;
+    q[e] = junction_q(a, t, e, j, w, th, a.Is, step);
   }
 }
 
-// b(p, w) = sum_j A_pj (x_j / c0_j - theta_s_j) - 2 pi f_p, p in the factor's face order
-__global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const double* __restrict__ xj,
+// b(p, w) = sum_j A_pj (q_j - theta_s_j) - 2 pi f_p, p in the factor's face order. Also
+// advances the device step counter (read by the junction evaluations of the next step).
+__global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const double* __restrict__ q,
                                                   double* __restrict__ b) {
   const int64_t NfW = (int64_t)a.Nf * a.W;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NfW; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = e / a.W, w = e - p * a.W;
     double acc = 0.0;
-    for (int64_t q = __ldg(t.fj_ptr + p); q < __ldg(t.fj_ptr + p + 1); ++q) {
-      const int64_t j = __ldg(t.fj_col + q);
-      double v = xj[j * a.W + w] * __ldg(t.inv_c0 + j);
+    for (int64_t i = __ldg(t.fj_ptr + p); i < __ldg(t.fj_ptr + p + 1); ++i) {
+      const int64_t j = __ldg(t.fj_col + i);
+      double v = q[j * a.W + w];
       if (a.theta_s) v -= a.theta_s[j * a.W + w];
-      acc = fma(__ldg(t.fj_val + q), v, acc);
+      acc = fma(__ldg(t.fj_val + i), v, acc);
     }
     if (a.f.ptr) acc -= kTwoPi * view_at(a.f, __ldg(t.face_orig + p), w);
     b[e] = acc;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *a.d_step += 1;
 }
 
-// theta_next = (A^T J - x)/c0, outputs, theta_s update (time_evolution.py:562-580)
-__global__ void __launch_bounds__(256) k_update(StepArgs a, Tables t, const double* __restrict__ xj,
-                                                const double* __restrict__ J, int64_t* d_step) {
+// theta_next = (A^T J)/c0 - q, outputs, theta_s update (time_evolution.py:562-580); with
+// `fuse_next` the same thread then evaluates q of the next step from the new history
+// (theta_next, h[0], ...), saving a pass over the phase arrays.
+template <bool kFuseNext>
+__global__ void __launch_bounds__(256) k_update(StepArgs a, Tables t, double* __restrict__ q,
+                                                const double* __restrict__ J) {
   const int64_t NjW = (int64_t)a.Nj * a.W;
+  const int64_t next_step = *a.d_step;   // already advanced by k_face_rhs
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = e / a.W, w = e - j * a.W;
     double y = 0.0;
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int p = __ldg(t.jf_face + 2 * j + q);
-      if (p >= 0) y = fma(__ldg(t.jf_val + 2 * j + q), J[(int64_t)p * a.W + w], y);
+    for (int i = 0; i < 2; ++i) {
+      const int p = __ldg(t.jf_face + 2 * j + i);
+      if (p >= 0) y = fma(__ldg(t.jf_val + 2 * j + i), J[(int64_t)p * a.W + w], y);
     }
-    const double th = (y - xj[e]) * __ldg(t.inv_c0 + j);
+    const double th = fma(y, __ldg(t.inv_c0 + j), -q[e]);
+    double hist[4];
+    if (kFuseNext) {
+      hist[0] = th;
+#pragma unroll
+      for (int k = 1; k < 4; ++k) hist[k] = (k < a.width - 1) ? a.h[k - 1][e] : 0.0;
+    }
     a.hout[e] = th;
     if (a.th_out && a.th_slot >= 0) a.th_out[a.th_slot * NjW + e] = th;
     if (a.I_out && a.I_slot >= 0) a.I_out[a.I_slot * NjW + e] = y + view_at(a.Is, j, w);
     if (a.theta_s && a.Vs.ptr) a.theta_s[e] += view_at(a.Vs, j, w) * a.dt;
+    if (kFuseNext) q[e] = junction_q(a, t, e, j, w, hist, a.Is, next_step);
   }
-  if (d_step && blockIdx.x == 0 && threadIdx.x == 0) *d_step += 1;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -220,8 +279,24 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, 
     const int r = r0 + rl + t * LG;
     rr[t] = r < r1 ? r : r0;
   }
+  // dot products over the supernode's columns; loads of kUnroll columns are issued before
+  // their FMAs so a warp keeps several L2 requests in flight (top levels have few warps)
   const int jend = min(k, r1);
-  for (int j = 0; j < jend; ++j) {
+  int j = 0;
+  for (; j + kUnroll <= jend; j += kUnroll) {
+    double bj[kUnroll], fv[kUnroll][kRowsPerLane];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) bj[u] = b[(int64_t)(c0 + j + u) * W + w];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+      for (int t = 0; t < kRowsPerLane; ++t) fv[u][t] = __ldg(Fs + (int64_t)(j + u) * nf + rr[t]);
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+      for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(fv[u][t], bj[u], acc[t]);
+  }
+  for (; j < jend; ++j) {
     const double bj = b[(int64_t)(c0 + j) * W + w];
     const double* col = Fs + (int64_t)j * nf;
 #pragma unroll
@@ -260,16 +335,49 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
     const int i = i0 + rl + t * LG;
     ii[t] = i < i1 ? i : i0;
   }
-  for (int r = i0; r < k; ++r) {
-    const double zr = z[(int64_t)(c0 + r) * W + w];
+  // diagonal block: inv(L11)^T z_s (zero above the diagonal, so start at row i0)
+  int r = i0;
+  for (; r + kUnroll <= k; r += kUnroll) {
+    double zr[kUnroll], fv[kUnroll][kRowsPerLane];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) zr[u] = __ldg(z + (int64_t)(c0 + r + u) * W + w);
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+      for (int t = 0; t < kRowsPerLane; ++t) fv[u][t] = __ldg(Fs + (int64_t)(r + u) * k + ii[t]);
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+      for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(fv[u][t], zr[u], acc[t]);
+  }
+  for (; r < k; ++r) {
+    const double zr = __ldg(z + (int64_t)(c0 + r) * W + w);
     const double* row = Fs + (int64_t)r * k;
 #pragma unroll
     for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(__ldg(row + ii[t]), zr, acc[t]);
   }
+  // off-diagonal rows: - (L21 inv(L11))^T x[R_s]; index loads, then value loads, then FMAs
   const int32_t* R = F.rows + __ldg(F.rowptr + s);
-  for (int r = 0; r < m; ++r) {
-    const double xr = x[(int64_t)__ldg(R + r) * W + w];
-    const double* row = Fs + (int64_t)(k + r) * k;
+  int q = 0;
+  for (; q + kUnroll <= m; q += kUnroll) {
+    int idx[kUnroll];
+    double xr[kUnroll], fv[kUnroll][kRowsPerLane];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) idx[u] = __ldg(R + q + u);
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+      for (int t = 0; t < kRowsPerLane; ++t) fv[u][t] = __ldg(Fs + (int64_t)(k + q + u) * k + ii[t]);
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) xr[u] = x[(int64_t)idx[u] * W + w];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+      for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(-fv[u][t], xr[u], acc[t]);
+  }
+  for (; q < m; ++q) {
+    const double xr = x[(int64_t)__ldg(R + q) * W + w];
+    const double* row = Fs + (int64_t)(k + q) * k;
 #pragma unroll
     for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(-__ldg(row + ii[t]), xr, acc[t]);
   }
@@ -279,6 +387,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
     if (i >= i1) break;
     x[(int64_t)(c0 + i) * W + w] = acc[t];
   }
+}
+
+__global__ void k_eval_sin(const double* __restrict__ x, double* __restrict__ out, int64_t n,
+                           const double2* __restrict__ tab) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = fast_sin(x[i], tab);
 }
 
 __global__ void k_permute_rows(const double* __restrict__ src, double* __restrict__ dst, const int32_t* __restrict__ map,
@@ -344,39 +458,8 @@ struct jja_plan {
 
 namespace {
 
-void launch_solve(jja_plan* p, cudaStream_t st) {
-  // forward: levels ascending (children before parents); b is consumed, z produced
-  for (int l = 0; l < p->n_levels; ++l) {
-    const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
-    if (!n) continue;
-    k_fwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
-        p->F, p->fwd_items + p->fwd_ptr[l], n, p->W, p->WB, p->b, p->z);
-    g_launches++;
-  }
-  // backward: levels descending; x produced
-  for (int l = p->n_levels - 1; l >= 0; --l) {
-    const int n = (int)(p->bwd_ptr[l + 1] - p->bwd_ptr[l]);
-    if (!n) continue;
-    k_bwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
-        p->F, p->bwd_items + p->bwd_ptr[l], n, p->W, p->WB, p->z, p->x);
-    g_launches++;
-  }
-}
-
-// one time step; hist rotation is done by the caller through `a`. With `ev` (6 events) the
-// stage boundaries junction | face rhs | forward | backward | update are recorded.
-void launch_step(jja_plan* p, StepArgs& a, cudaStream_t st, cudaEvent_t* ev = nullptr) {
-  const int64_t NjW = (int64_t)p->Nj * p->W, NfW = (int64_t)p->Nf * p->W;
-  if (ev) JJA_CUDA(cudaEventRecord(ev[0], st));
-  k_junction<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj);
-  if (ev) JJA_CUDA(cudaEventRecord(ev[1], st));
-  k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(a, p->t, p->xj, p->b);
-  if (ev) JJA_CUDA(cudaEventRecord(ev[2], st));
-  g_launches += 2;
-  if (!ev) {
-    launch_solve(p, st);
-  } else {
-    // forward and backward separately so both can be timed
+void launch_levels(jja_plan* p, cudaStream_t st, bool forward) {
+  if (forward) {  // levels ascending (children before parents); b is consumed, z produced
     for (int l = 0; l < p->n_levels; ++l) {
       const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
       if (!n) continue;
@@ -384,7 +467,7 @@ void launch_step(jja_plan* p, StepArgs& a, cudaStream_t st, cudaEvent_t* ev = nu
           p->F, p->fwd_items + p->fwd_ptr[l], n, p->W, p->WB, p->b, p->z);
       g_launches++;
     }
-    JJA_CUDA(cudaEventRecord(ev[3], st));
+  } else {        // levels descending; x produced
     for (int l = p->n_levels - 1; l >= 0; --l) {
       const int n = (int)(p->bwd_ptr[l + 1] - p->bwd_ptr[l]);
       if (!n) continue;
@@ -392,11 +475,31 @@ void launch_step(jja_plan* p, StepArgs& a, cudaStream_t st, cudaEvent_t* ev = nu
           p->F, p->bwd_items + p->bwd_ptr[l], n, p->W, p->WB, p->z, p->x);
       g_launches++;
     }
-    JJA_CUDA(cudaEventRecord(ev[4], st));
   }
-  k_update<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj, p->x, p->d_step);
+}
+
+// q of the first step of a run, from the phase history
+void launch_junction(jja_plan* p, StepArgs& a, cudaStream_t st) {
+  k_junction<<<grid_for((int64_t)p->Nj * p->W, 256), 256, 0, st>>>(a, p->t, p->xj);
   g_launches++;
-  if (ev) JJA_CUDA(cudaEventRecord(ev[5], st));
+}
+
+// one time step whose q is already in p->xj; `fuse_next` also leaves the next step's q there.
+// With `ev` (5 events) the boundaries face rhs | forward | backward | update(+next q) are recorded.
+void launch_step(jja_plan* p, StepArgs& a, cudaStream_t st, bool fuse_next, cudaEvent_t* ev = nullptr) {
+  const int64_t NjW = (int64_t)p->Nj * p->W, NfW = (int64_t)p->Nf * p->W;
+  if (ev) JJA_CUDA(cudaEventRecord(ev[0], st));
+  k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(a, p->t, p->xj, p->b);
+  g_launches++;
+  if (ev) JJA_CUDA(cudaEventRecord(ev[1], st));
+  launch_levels(p, st, true);
+  if (ev) JJA_CUDA(cudaEventRecord(ev[2], st));
+  launch_levels(p, st, false);
+  if (ev) JJA_CUDA(cudaEventRecord(ev[3], st));
+  if (fuse_next) k_update<true><<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj, p->x);
+  else k_update<false><<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj, p->x);
+  g_launches++;
+  if (ev) JJA_CUDA(cudaEventRecord(ev[4], st));
 }
 
 StepArgs make_args(jja_plan* p, jja_state* s) {
@@ -439,6 +542,8 @@ int jja_factor_create(int n, const int64_t* colptr, const int32_t* rowind, const
       if (opts->nd_leaf > 0) o.nd_leaf = opts->nd_leaf;
       o.max_supernode = opts->max_supernode;
       o.keep_factor = opts->keep_factor;
+      if (opts->relax_zeros >= 0) o.relax_zeros = opts->relax_zeros;
+      if (opts->relax_frac >= 0.0) o.relax_frac = opts->relax_frac;
     }
     std::unique_ptr<jja_factor> f(new jja_factor);
     try {
@@ -472,6 +577,19 @@ int jja_factor_get_perm(const jja_factor* f, int32_t* perm_out) {
   return guarded([&] {
     if (!f || !perm_out) throw Error(JJA_ERR_ARG, "null argument");
     std::copy(f->f->perm.begin(), f->f->perm.end(), perm_out);
+  });
+}
+
+int jja_factor_get_supernodes(const jja_factor* f, int32_t* col0, int32_t* k, int32_t* m, int32_t* level,
+                              int32_t* parent) {
+  return guarded([&] {
+    if (!f) throw Error(JJA_ERR_ARG, "null factor");
+    const jja::Factor& F = *f->f;
+    if (col0) std::copy(F.sn_col0.begin(), F.sn_col0.end(), col0);
+    if (k) std::copy(F.sn_k.begin(), F.sn_k.end(), k);
+    if (m) std::copy(F.sn_m.begin(), F.sn_m.end(), m);
+    if (level) std::copy(F.sn_level.begin(), F.sn_level.end(), level);
+    if (parent) std::copy(F.sn_parent.begin(), F.sn_parent.end(), parent);
   });
 }
 
@@ -528,6 +646,20 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->t.jf_face = p->up(jf_face.data(), jf_face.size());
     p->t.jf_val = p->up(jf_val.data(), jf_val.size());
     p->perm = p->up(F.perm.data(), F.perm.size());
+    {
+      // sin/cos of k pi/2048: first-quadrant values in extended precision, rounded once to
+      // double, then exact quadrant symmetries, so sin(m pi) and cos(m pi + pi/2) are exactly 0
+      std::vector<double2> tab(kSinTable);
+      const long double pi_l = 3.141592653589793238462643383279502884L;
+      for (int k = 0; k < kSinTable; ++k) {
+        const int q = k / 1024, r = k % 1024;
+        const long double ang = (long double)r * pi_l / 2048.0L;
+        const double s0 = (double)sinl(ang), c0 = (double)cosl(ang);
+        const double sv[4] = {s0, c0, -s0, -c0}, cv[4] = {c0, -s0, -c0, s0};
+        tab[k] = make_double2(sv[q], cv[q]);
+      }
+      p->t.sincos = p->up(tab.data(), tab.size());
+    }
     // factor blocks (column-major copy for the forward pass, row-major for the backward pass)
     std::vector<double> frow(F.fcol.size());
     for (int s = 0; s < F.ns; ++s) {
@@ -589,8 +721,19 @@ int jja_solve(jja_plan* p, const double* b, double* x, void* stream) {
     const int64_t NfW = (int64_t)p->Nf * p->W;
     k_permute_rows<<<grid_for(NfW, 256), 256, 0, st>>>(b, p->b, p->perm, p->Nf, p->W, 1);
     g_launches++;
-    launch_solve(p, st);
+    launch_levels(p, st, true);
+    launch_levels(p, st, false);
     k_permute_rows<<<grid_for(NfW, 256), 256, 0, st>>>(p->x, x, p->perm, p->Nf, p->W, 0);
+    g_launches++;
+    JJA_CUDA(cudaGetLastError());
+  });
+}
+
+int jja_eval_sin(jja_plan* p, const double* x, double* out, int64_t n, void* stream) {
+  return guarded([&] {
+    if (!p || !x || !out || n < 0) throw Error(JJA_ERR_ARG, "jja_eval_sin: bad arguments");
+    if (n == 0) return;
+    k_eval_sin<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(x, out, n, p->t.sincos);
     g_launches++;
     JJA_CUDA(cudaGetLastError());
   });
@@ -603,8 +746,15 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
     for (int k = 0; k < p->width - 1; ++k)
       if (!s->hist[k]) throw Error(JJA_ERR_ARG, "jja_run: missing history buffer");
     if (s->noise_mode == JJA_NOISE_BUFFER && !s->noise) throw Error(JJA_ERR_ARG, "jja_run: noise buffer missing");
+    if (nsteps == 0) return;
     cudaStream_t st = (cudaStream_t)stream;
     JJA_CUDA(cudaMemcpyAsync(p->d_step, &s->step, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    {
+      StepArgs a = make_args(p, s);
+      launch_junction(p, a, st);
+    }
+    // one-step calls come from a host loop that changes sources between steps: no fusion
+    const bool fuse = nsteps > 1;
     const int period = p->width - 1;  // history rotation period
     int i = 0;
     while (i < nsteps) {
@@ -613,7 +763,7 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
       while (i + run < nsteps && (!th_slot || th_slot[i + run] < 0) && (!I_slot || I_slot[i + run] < 0)) ++run;
       const int G = 16 * period;
       // capture needs a non-default stream; the per-step noise buffer is refilled by the host
-      if (use_graph && st != nullptr && run >= G && s->noise_mode != JJA_NOISE_BUFFER) {
+      if (use_graph && fuse && st != nullptr && run >= G && s->noise_mode != JJA_NOISE_BUFFER) {
         std::vector<uint64_t> key = {(uint64_t)s->hist[0], (uint64_t)s->hist[1], (uint64_t)s->hist[2],
                                      (uint64_t)s->hist[3], (uint64_t)s->theta_s, (uint64_t)s->Is.ptr,
                                      (uint64_t)s->f.ptr, (uint64_t)s->Vs.ptr, (uint64_t)s->T.ptr,
@@ -631,7 +781,7 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
             StepArgs a = make_args(p, &tmp);
             a.hout = tmp.hist[period - 1];
             a.th_slot = a.I_slot = -1;
-            launch_step(p, a, st);
+            launch_step(p, a, st, true);
             rotate(&tmp, p->width);
           }
           JJA_CUDA(cudaStreamEndCapture(st, &g));
@@ -650,7 +800,7 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
         a.hout = s->hist[period - 1];
         a.th_slot = th_slot ? th_slot[i] : -1;
         a.I_slot = I_slot ? I_slot[i] : -1;
-        launch_step(p, a, st);
+        launch_step(p, a, st, fuse);
         rotate(s, p->width);
       }
     }
@@ -665,29 +815,35 @@ int jja_run_timed(jja_plan* p, jja_state* s, int nsteps, double* stage_ms, void*
     if (s->noise_mode == JJA_NOISE_BUFFER) throw Error(JJA_ERR_ARG, "jja_run_timed: host noise buffer not supported");
     cudaStream_t st = (cudaStream_t)stream;
     JJA_CUDA(cudaMemcpyAsync(p->d_step, &s->step, sizeof(int64_t), cudaMemcpyHostToDevice, st));
-    std::vector<cudaEvent_t> ev(6 * (size_t)nsteps);
+    std::vector<cudaEvent_t> ev(1 + 5 * (size_t)nsteps);
     for (auto& e : ev) JJA_CUDA(cudaEventCreate(&e));
+    JJA_CUDA(cudaEventRecord(ev[0], st));
+    {
+      StepArgs a = make_args(p, s);
+      launch_junction(p, a, st);
+    }
     const int period = p->width - 1;
     for (int i = 0; i < nsteps; ++i) {
       StepArgs a = make_args(p, s);
       a.hout = s->hist[period - 1];
       a.th_slot = a.I_slot = -1;
-      launch_step(p, a, st, ev.data() + 6 * (size_t)i);
+      launch_step(p, a, st, true, ev.data() + 1 + 5 * (size_t)i);
       rotate(s, p->width);
     }
     JJA_CUDA(cudaEventSynchronize(ev.back()));
     for (int k = 0; k < 6; ++k) stage_ms[k] = 0.0;
+    float ms = 0.f;
+    JJA_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+    stage_ms[0] = ms;  // first junction evaluation
     for (int i = 0; i < nsteps; ++i) {
-      const cudaEvent_t* e = ev.data() + 6 * (size_t)i;
-      for (int k = 0; k < 5; ++k) {
-        float ms = 0.f;
+      const cudaEvent_t* e = ev.data() + 1 + 5 * (size_t)i;
+      for (int k = 0; k < 4; ++k) {
         JJA_CUDA(cudaEventElapsedTime(&ms, e[k], e[k + 1]));
-        stage_ms[k] += ms;
+        stage_ms[1 + k] += ms;
       }
     }
-    float total = 0.f;
-    JJA_CUDA(cudaEventElapsedTime(&total, ev.front(), ev.back()));
-    stage_ms[5] = total;
+    JJA_CUDA(cudaEventElapsedTime(&ms, ev.front(), ev.back()));
+    stage_ms[5] = ms;
     for (auto& e : ev) cudaEventDestroy(e);
     s->step += nsteps;
   });

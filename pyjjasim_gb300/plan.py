@@ -60,7 +60,8 @@ def face_matrix(circuit, dt):
 class HostFactor:
     """Ordered supernodal Cholesky of K (owned C object)."""
 
-    def __init__(self, K, coords=None, perm=None, nd_leaf=8, max_supernode=0, keep_factor=False):
+    def __init__(self, K, coords=None, perm=None, nd_leaf=8, max_supernode=0, keep_factor=False, relax_zeros=-1,
+                 relax_frac=-1.0):
         L = N.lib()
         n = K.shape[0]
         self.n = n
@@ -72,7 +73,7 @@ class HostFactor:
             cx = np.ascontiguousarray(coords[0], np.float64)
             cy = np.ascontiguousarray(coords[1], np.float64)
         pm = None if perm is None else np.ascontiguousarray(perm, np.int32)
-        opts = N.FactorOpts(nd_leaf, max_supernode, int(keep_factor))
+        opts = N.FactorOpts(nd_leaf, max_supernode, int(keep_factor), int(relax_zeros), float(relax_frac))
         h = ctypes.c_void_p()
         N.check(L.jja_factor_create(n, N.ptr(colptr, ctypes.c_int64), N.ptr(rowind, ctypes.c_int32), N.ptr(val),
                                     N.ptr(cx), N.ptr(cy), N.ptr(pm, ctypes.c_int32), ctypes.byref(opts),
@@ -85,6 +86,14 @@ class HostFactor:
     def perm(self):
         out = np.empty(self.n, np.int32)
         N.check(N.lib().jja_factor_get_perm(self.handle, N.ptr(out, ctypes.c_int32)))
+        return out
+
+    def supernodes(self):
+        """dict of per-supernode arrays: col0, k, m, level, parent."""
+        ns = self.stats["n_supernodes"]
+        out = {k: np.empty(ns, np.int32) for k in ("col0", "k", "m", "level", "parent")}
+        N.check(N.lib().jja_factor_get_supernodes(self.handle, *(N.ptr(out[k], ctypes.c_int32)
+                                                                for k in ("col0", "k", "m", "level", "parent"))))
         return out
 
     def solve_host(self, b):
@@ -130,6 +139,10 @@ class DevicePlan:
 
     def solve(self, b_dev, x_dev, stream=0):
         N.check(N.lib().jja_solve(self.handle, ctypes.c_void_p(b_dev), ctypes.c_void_p(x_dev), ctypes.c_void_p(stream)))
+
+    def eval_sin(self, x_dev, out_dev, n, stream=0):
+        N.check(N.lib().jja_eval_sin(self.handle, ctypes.c_void_p(x_dev), ctypes.c_void_p(out_dev), int(n),
+                                     ctypes.c_void_p(stream)))
 
     def __del__(self):
         h = getattr(self, "handle", None)
