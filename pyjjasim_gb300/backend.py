@@ -38,6 +38,21 @@ def _is_default_cpr(cpr):
     return type(cpr).__name__ == "DefaultCPR"
 
 
+def _compact(v):
+    """The non-broadcast part of a 2-D view: axes with stride 0 shrink to length 1."""
+    return v[:1 if v.strides[0] == 0 else v.shape[0], :1 if v.strides[1] == 0 else v.shape[1]]
+
+
+def _source_is_zero(timedep, getter, N_rows, W):
+    """The reference's zero test ``np.allclose(x, 0)`` for time-independent sources
+    (time_evolution.py:512-519), evaluated on the non-broadcast part: |x| <= 1e-8 everywhere
+    (NaN and inf are not close to 0)."""
+    if timedep:
+        return False
+    v = _compact(np.broadcast_to(np.asarray(getter(0), dtype=np.float64), (N_rows, W)))
+    return bool(np.all(np.abs(v) <= 1e-8))
+
+
 class _Source:
     """A source (Is, f, Vs or T) on the device as a strided view, updated per step if time-dependent."""
 
@@ -53,8 +68,7 @@ class _Source:
         if timedep:
             rows, cols = N_rows, W        # a later step may not broadcast like step 0: keep it full
         else:
-            rows = 1 if v0.strides[0] == 0 else N_rows
-            cols = 1 if v0.strides[1] == 0 else W
+            rows, cols = _compact(v0).shape
         self.shape = (rows, cols)
         self.buf = torch.empty(self.shape, dtype=torch.float64, device=dev)
         self.view = N.View(self.buf.data_ptr(), cols if rows > 1 else 0, 1 if cols > 1 else 0)
@@ -116,20 +130,25 @@ class GpuSimulation:
             if self.width >= 5:
                 hist0.append(problem.config_at_minus_4)
             self.hist0 = hist0
+            self.hist0_zero = []
+            self.hist = []
             with torch.cuda.stream(self.stream):
-                host = [np.ascontiguousarray(np.broadcast_to(h, (self.Nj, self.W)), np.float64) for h in hist0]
-                self.hist = [torch.from_numpy(h).to(self.dev) for h in host]
-                self.h2d_bytes += sum(h.nbytes for h in host)
-
-            def is_zero(timedep, getter):     # zero detection as in time_evolution.py:509-519
-                return (not timedep) and bool(np.allclose(getter(0), 0))
-
+                for h in hist0:
+                    h = np.ascontiguousarray(np.broadcast_to(h, (self.Nj, self.W)), np.float64)
+                    zero = not np.any(h)
+                    self.hist0_zero.append(zero)
+                    if zero:      # the default initial condition: no host->device copy needed
+                        self.hist.append(torch.zeros((self.Nj, self.W), dtype=torch.float64, device=self.dev))
+                    else:
+                        self.hist.append(torch.from_numpy(h).to(self.dev))
+                        self.h2d_bytes += h.nbytes
             self.srcs = {}
             for name, getter, td, rows in (("Is", problem._Is, problem._Is_is_timedep, self.Nj),
                                            ("f", problem._f, problem._f_is_timedep, self.Nf),
                                            ("Vs", problem._Vs, problem._Vs_is_timedep, self.Nj),
                                            ("T", problem._T, problem._T_is_timedep, self.Nj)):
-                self.srcs[name] = _Source(torch, self.dev, self.stream, getter, td, rows, self.W, is_zero(td, getter))
+                zero = _source_is_zero(td, getter, rows, self.W)
+                self.srcs[name] = _Source(torch, self.dev, self.stream, getter, td, rows, self.W, zero)
             self.h2d_bytes += sum(s.h2d_bytes for s in self.srcs.values())
             Vs_zero, T_zero = self.srcs["Vs"].zero, self.srcs["T"].zero
             self.theta_s = None if Vs_zero else torch.zeros((self.Nj, self.W), dtype=torch.float64, device=self.dev)
@@ -218,11 +237,16 @@ def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", se
     I_store_mask = np.asarray(I_store_mask, bool)
     n_init = width - 1
     n_th, n_I = int(th_store_mask.sum()), int(I_store_mask.sum())
-    th_out = np.zeros((Nj, W, n_th + n_init))
-    I_out = np.zeros((Nj, W, n_I + n_init))
-    for lag, th in enumerate(sim.hist0):     # initial conditions (time_evolution.py:480-502)
-        th_out[:, :, n_init - 1 - lag] = th
-        I_out[:, :, n_init - 1 - lag] = problem._cp(th)
+    # outputs are filled time-major, one contiguous (Nj, W) block per slot, and returned as
+    # (Nj, W, slots) views: the shape and values of the reference's arrays without a transpose
+    th_buf = np.empty((n_th + n_init, Nj, W))
+    I_buf = np.empty((n_I + n_init, Nj, W))
+    for lag, (th, zero) in enumerate(zip(sim.hist0, sim.hist0_zero)):   # time_evolution.py:480-502
+        th_buf[n_init - 1 - lag] = th
+        if zero:
+            I_buf[n_init - 1 - lag] = 0.0          # cp(0) = Ic sin 0
+        else:
+            I_buf[n_init - 1 - lag] = problem._cp(np.broadcast_to(th, (Nj, W)))
     th_idx = np.where(th_store_mask, np.cumsum(th_store_mask) - 1, -1).astype(np.int64)
     I_idx = np.where(I_store_mask, np.cumsum(I_store_mask) - 1, -1).astype(np.int64)
     max_slots = max(1, _MAX_OUT_BYTES // (2 * Nj * W * 8))
@@ -244,12 +268,12 @@ def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", se
             sim.run(i1 - i0, seg_th, seg_I, th_dev, I_dev, use_graph=use_graph)
             sim.synchronize()
             if cnt_th:
-                th_out[:, :, n_init + base_th:n_init + base_th + cnt_th] = th_dev.cpu().numpy().transpose(1, 2, 0)
+                torch.from_numpy(th_buf[n_init + base_th:n_init + base_th + cnt_th]).copy_(th_dev)
             if cnt_I:
-                I_out[:, :, n_init + base_I:n_init + base_I + cnt_I] = I_dev.cpu().numpy().transpose(1, 2, 0)
+                torch.from_numpy(I_buf[n_init + base_I:n_init + base_I + cnt_I]).copy_(I_dev)
             del th_dev, I_dev
             i0 = i1
-    return th_out, I_out
+    return th_buf.transpose(1, 2, 0), I_buf.transpose(1, 2, 0)
 
 
 def solve_faces(circuit, dt, b, stencil_width=3, nd_leaf=8):

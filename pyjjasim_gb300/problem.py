@@ -210,16 +210,31 @@ class TimeEvolutionProblem:
         return time_points
 
 
-def _stencil_derivative(x, index, s1, dt):
-    out = s1[0] * x[:, :, index]
+def _stencil_derivative(x_tm, index, s1, dt):
+    """Backward-stencil derivative at stored slots ``index`` of a time-major (slots, Nj, W)
+    array, returned time-major (time_evolution.py:411-420, same operation order)."""
+    out = s1[0] * x_tm[index]
     for k in range(1, len(s1) - 1):
-        out = out + s1[k] * x[:, :, index - k]
+        out = out + s1[k] * x_tm[index - k]
     return out / dt
 
 
-def time_evolution(problem, **options):
-    """Driver around the GPU core: masks, core call, voltage (time_evolution.py:422-458)."""
-    from .backend import time_evolution_core
+def _select_slots(x, slots):
+    """x[:, :, slots] for a (Nj, W, S) array, kept as a view of its time-major storage when
+    the slots form a contiguous range."""
+    tm = x.transpose(2, 0, 1)
+    if len(slots) and np.all(np.diff(slots) == 1):
+        return tm[slots[0]:slots[-1] + 1].transpose(1, 2, 0)
+    return tm[slots].transpose(1, 2, 0)
+
+
+def time_evolution(problem, core=None, **options):
+    """Driver around the GPU core: masks, core call, voltage (time_evolution.py:422-458).
+
+    ``core`` replaces the GPU core with another function of the same signature (tests use
+    this to check the masks and post-processing on a machine without a GPU)."""
+    if core is None:
+        from .backend import time_evolution_core as core
     Nt = problem._Nt()
     store = np.asarray(problem.store_time_steps, bool)
     th_mask = store.copy() if (problem.store_theta or problem.store_voltage) else np.zeros(Nt, bool)
@@ -234,19 +249,25 @@ def time_evolution(problem, **options):
         Vth_mask[ids] = True
         if c._has_inductance():
             VI_mask[ids] = True
-    th_out, I_out = time_evolution_core(problem, Vth_mask, VI_mask, **options)
+    th_out, I_out = core(problem, Vth_mask, VI_mask, **options)
     V = None
     if problem.store_voltage:
         ts = np.flatnonzero(store[Vth_mask])
-        V = _stencil_derivative(th_out, ts + offset, problem.stencil[0], problem._dt())
+        s1, dt = problem.stencil[0], problem._dt()
+        V = _stencil_derivative(th_out.transpose(2, 0, 1), ts + offset, s1, dt)
         if c._has_inductance():
-            VI = _stencil_derivative(I_out, ts + offset, problem.stencil[0], problem._dt())
-            V = V + (c.get_inductance() @ VI.reshape((c._Nj(), -1))).reshape(V.shape)
-        th_out = np.delete(th_out, np.flatnonzero((Vth_mask & ~th_mask)[Vth_mask]) + offset, axis=2)
-        I_out = np.delete(I_out, np.flatnonzero((VI_mask & ~I_mask)[VI_mask]) + offset, axis=2)
-    th_out, I_out = th_out[:, :, offset:], I_out[:, :, offset:]
-    return TimeEvolutionResult(problem, th_out if problem.store_theta else None,
-                               I_out if problem.store_current else None, V)
+            VI = _stencil_derivative(I_out.transpose(2, 0, 1), ts + offset, s1, dt)
+            Nj = c._Nj()
+            VI = np.ascontiguousarray(VI.transpose(1, 2, 0)).reshape((Nj, -1))
+            V = V + (c.get_inductance() @ VI).reshape((Nj, -1, len(ts))).transpose(2, 0, 1)
+        V = V.transpose(1, 2, 0)
+    # keep the slots of steps stored for their own sake (the reference deletes the helper
+    # slots and the initial conditions, time_evolution.py:451-455)
+    th_keep = offset + np.flatnonzero(th_mask[Vth_mask])
+    I_keep = offset + np.flatnonzero(I_mask[VI_mask])
+    th_out = _select_slots(th_out, th_keep) if problem.store_theta else None
+    I_out = _select_slots(I_out, I_keep) if problem.store_current else None
+    return TimeEvolutionResult(problem, th_out, I_out, V)
 
 
 class ThetaNotStored(Exception):
