@@ -144,6 +144,20 @@ int jja_run_timed(jja_plan* p, jja_state* st, int nsteps, double* stage_ms, void
  * Nf x W, original face order). Exposed for tests of the triangular-solve kernels. */
 int jja_solve(jja_plan* p, const double* b, double* x, void* stream);
 
+/* Allocation-free variant of jja_solve. No counterpart in the reference: it exists for callers
+ * that cannot allocate device memory when they solve — code running after all device memory has
+ * been handed to another allocator (a framework's caching pool) or under a hard memory budget,
+ * and per-step loops that must not pay the device-wide synchronisation of cudaMalloc/cudaFree.
+ * It uses the plan's factor tables and, instead of the plan's work vectors, a fixed 32 MiB
+ * device array inside the library (held by every GPU that loads the library until exit); it
+ * calls no cudaMalloc, cudaFree or allocating library routine. Limit: 2 x Nf x W doubles must fit,
+ * i.e. Nf * W <= 2,097,152 (for example a 128 x 128 array with W <= 130); larger plans get
+ * JJA_ERR_ARG with the limit in the message. The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (different streams or threads) race.
+ * b and x are caller-owned device arrays (Nf x W, original face order), as for jja_solve. */
+int jja_solve_static(jja_plan* p, const double* b, double* x, void* stream);
+
 /* out[i] = sin(x[i]) with the library's device sine (device arrays of n doubles), the one
  * the junction-current kernels use for Ic sin(theta) (pyjjasim static_problem.py:82-85).
  * Exposed so tests can bound its error against a correctly rounded sine. */

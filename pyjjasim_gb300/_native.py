@@ -60,6 +60,7 @@ SIGNATURES = {
     "jja_run": (c_int, [c_void_p, ctypes.POINTER(State), c_int, P_i64, P_i64, c_int, c_void_p]),
     "jja_run_timed": (c_int, [c_void_p, ctypes.POINTER(State), c_int, P_f64, c_void_p]),
     "jja_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "jja_solve_static": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "jja_eval_sin": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
     "jja_last_error": (ctypes.c_char_p, []),
     "jja_launch_count": (c_int64, []),

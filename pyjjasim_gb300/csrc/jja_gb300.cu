@@ -20,6 +20,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <mutex>
 #include <vector>
 
 namespace {
@@ -724,6 +725,83 @@ int jja_solve(jja_plan* p, const double* b, double* x, void* stream) {
     launch_levels(p, st, true);
     launch_levels(p, st, false);
     k_permute_rows<<<grid_for(NfW, 256), 256, 0, st>>>(p->x, x, p->perm, p->Nf, p->W, 0);
+    g_launches++;
+    JJA_CUDA(cudaGetLastError());
+  });
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// Allocation-free face-space solve (jja_solve_static). Its two work vectors live in this
+// file-scope device array instead of memory from cudaMalloc: 32 MiB that every GPU which loads
+// the library holds until the process exits. Host code must not use the array's name as a
+// device address; the address is looked up once per device with cudaGetSymbolAddress.
+// ------------------------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t kStaticScratchDoubles = int64_t(4) << 20;   // 32 MiB
+__device__ __align__(256) double g_static_scratch[kStaticScratchDoubles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+double* g_static_ptr[kMaxDevices] = {};
+
+double* static_scratch_for_current_device() {
+  int dev = 0;
+  JJA_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) throw Error(JJA_ERR_ARG, "jja_solve_static: device index out of range");
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_ptr[dev]) {
+    void* ptr = nullptr;
+    JJA_CUDA(cudaGetSymbolAddress(&ptr, g_static_scratch));
+    g_static_ptr[dev] = static_cast<double*>(ptr);
+  }
+  return g_static_ptr[dev];
+}
+
+// the level sweeps of launch_levels with explicit work vectors
+void launch_levels_into(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x) {
+  if (forward) {
+    for (int l = 0; l < p->n_levels; ++l) {
+      const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
+      if (!n) continue;
+      k_fwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
+          p->F, p->fwd_items + p->fwd_ptr[l], n, p->W, p->WB, b, z);
+      g_launches++;
+    }
+  } else {
+    for (int l = p->n_levels - 1; l >= 0; --l) {
+      const int n = (int)(p->bwd_ptr[l + 1] - p->bwd_ptr[l]);
+      if (!n) continue;
+      k_bwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
+          p->F, p->bwd_items + p->bwd_ptr[l], n, p->W, p->WB, z, x);
+      g_launches++;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int jja_solve_static(jja_plan* p, const double* b, double* x, void* stream) {
+  return guarded([&] {
+    if (!p || !b || !x) throw Error(JJA_ERR_ARG, "jja_solve_static: null argument");
+    const int64_t NfW = (int64_t)p->Nf * p->W;
+    if (2 * NfW > kStaticScratchDoubles)
+      throw Error(JJA_ERR_ARG, "jja_solve_static: faces x problems = " + std::to_string(NfW) +
+                                   " exceeds the static scratch limit of " +
+                                   std::to_string(kStaticScratchDoubles / 2) + " (32 MiB for two work vectors)");
+    double* bx = static_scratch_for_current_device();   // permuted right-hand side, later the solution
+    double* z = bx + NfW;                              // forward-substitution result
+    cudaStream_t st = (cudaStream_t)stream;
+    // every element of both work vectors is written before it is read: nothing to clear
+    k_permute_rows<<<grid_for(NfW, 256), 256, 0, st>>>(b, bx, p->perm, p->Nf, p->W, 1);
+    g_launches++;
+    launch_levels_into(p, st, true, bx, z, nullptr);
+    launch_levels_into(p, st, false, nullptr, z, bx);
+    k_permute_rows<<<grid_for(NfW, 256), 256, 0, st>>>(bx, x, p->perm, p->Nf, p->W, 0);
     g_launches++;
     JJA_CUDA(cudaGetLastError());
   });
