@@ -115,12 +115,33 @@ struct Tables {
   const double* Rv;
   const int64_t* fj_ptr;   // permuted face -> junction entries
   const int32_t* fj_col;
-  const double* fj_val;
   const int32_t* face_orig;
-  const int32_t* jf_face;  // 2 per junction (permuted face or -1)
-  const double* jf_val;
-  const double2* sincos;   // {sin, cos}(k pi / 2048), k < 4096
+  const int32_t* jf_face;  // 2 per junction: (permuted face << 1) | (A entry is -1), or -1
+  const double2* sincos;   // per k < 4096: {S, C}, {-S/2, (float S, float C)}; S, C = sin, cos(k pi/2048)
 };
+
+// FP64 <-> FP32 conversions by bit manipulation on the integer pipe: on GB300 the conversion
+// instructions share the narrow FP64 pipe. Valid for |v| in [2^-126, 2^128); smaller values
+// flush to signed zero (callers only convert small correction terms).
+__device__ __forceinline__ float f32_from_f64(double v) {
+  const unsigned hi = (unsigned)__double2hiint(v), lo = (unsigned)__double2loint(v);
+  const int e = (int)((hi >> 20) & 0x7ffu);
+  unsigned bits = (hi & 0x80000000u) | ((unsigned)(e - 896) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  bits += (lo >> 28) & 1u;                    // round half away from zero on the magnitude
+  return __uint_as_float((e > 896 && e < 1151) ? bits : (hi & 0x80000000u));
+}
+
+__device__ __forceinline__ double f64_from_f32(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+  return e ? __hiloint2double((int)hi, (int)(b << 29)) : 0.0;
+}
+
+// +-v by flipping the sign bit (no FP64 instruction)
+__device__ __forceinline__ double signed_by(double v, int neg) {
+  return __hiloint2double(__double2hiint(v) ^ (neg << 31), __double2loint(v));
+}
 
 // ------------------------------------------------------------------------------------------
 // sin(x) in FP64 with few FP64 instructions (GB300's FP64 pipe is ~60x narrower than FP32).
@@ -129,8 +150,9 @@ struct Tables {
 //   sin(x) = S + C t - S t^2/2 - C t^3/6 + S t^4/24 + O(t^5),  S, C = sin, cos(k pi/2048),
 // from a 4096-entry table computed on the host in extended precision. |t^3/6| < 7.6e-11 and
 // |t^4/24| < 1.5e-14, so those two terms are evaluated in FP32 (absolute error < 2e-17);
-// the rest is three FP64 FMAs. The O(t^5) remainder is below 3e-18. |x| >= 2e5 (or NaN)
-// falls back to the CUDA math library.
+// the rest is two FP64 FMAs (the table also holds -S/2). The O(t^5) remainder is below 3e-18.
+// |x| >= 2e5, inf and NaN fall back to the CUDA math library (range test on the integer pipe).
+// Nine FP64 instructions in all.
 // ------------------------------------------------------------------------------------------
 constexpr double kSinScale = 0x1.45f306dc9c883p+9;   // 2048 / pi
 constexpr double kSinC1 = 0x1.921fb58000000p-10;
@@ -140,43 +162,51 @@ constexpr double kRoundMagic = 6755399441055744.0;   // 1.5 * 2^52: adding it ro
 constexpr int kSinTable = 4096;
 
 __device__ __forceinline__ double fast_sin(double x, const double2* __restrict__ tab) {
-  if (!(fabs(x) < 2.0e5)) return sin(x);
+  if ((__double2hiint(x) & 0x7fffffff) >= 0x41086A00) return sin(x);   // |x| >= 2e5, inf, NaN
   const double s = fma(x, kSinScale, kRoundMagic);
-  const int k = __double2loint(s);
+  const int k = __double2loint(s) & (kSinTable - 1);
   const double kd = s - kRoundMagic;
   double t = fma(-kd, kSinC1, x);
   t = fma(-kd, kSinC2, t);
   t = fma(-kd, kSinC3, t);
-  const double2 sc = __ldg(tab + (k & (kSinTable - 1)));
-  const double mh = (-0.5 * t) * t;          // -t^2/2
-  double r = fma(sc.y, t, sc.x);             // S + C t
-  r = fma(sc.x, mh, r);                      // - S t^2/2
-  const float tf = __double2float_rn(t);
+  const double2 sc = __ldg(tab + 2 * k);       // S, C
+  const double2 hv = __ldg(tab + 2 * k + 1);   // -S/2, packed float S and C
+  double r = fma(sc.y, t, sc.x);               // S + C t
+  r = fma(hv.x, t * t, r);                     // - S t^2/2
+  const float sf = __int_as_float(__double2loint(hv.y)), cf = __int_as_float(__double2hiint(hv.y));
+  const float tf = f32_from_f64(t);
   const float t2 = tf * tf;
-  const float tail = fmaf(__double2float_rn(sc.x) * (1.0f / 24.0f), t2 * t2,
-                          -(__double2float_rn(sc.y) * (1.0f / 6.0f)) * (t2 * tf));
-  return r + (double)tail;
+  const float tail = fmaf(sf * (1.0f / 24.0f), t2 * t2, -(cf * (1.0f / 6.0f)) * (t2 * tf));
+  return r + f64_from_f32(tail);
 }
 
 // q(j, w) = x / c0 for the step whose phase history is th[0..] (time_evolution.py:533-558):
 //   x = sqrt(2 T Rv) xi - Is + Ic sin(sum_k e_k th_k) + sum_k c_k th_k
 __device__ __forceinline__ double junction_q(const StepArgs& a, const Tables& t, int64_t e, int64_t j, int64_t w,
                                             const double* th, const jja_view& Is, int64_t step) {
-  double arg = 0.0;
+  double arg;
+  if (a.width == 3) {
+    arg = fma(2.0, th[0], -th[1]);        // 2 th1 - th2 with the reference's single rounding
+  } else {
+    arg = a.e[0] * th[0];
 #pragma unroll
-  for (int k = 0; k < 4; ++k)
-    if (k < a.width - 1) arg = fma(a.e[k], th[k], arg);
+    for (int k = 1; k < 4; ++k)
+      if (k < a.width - 1) arg = fma(a.e[k], th[k], arg);
+  }
   double X = __ldg(t.Ic + j) * fast_sin(arg, t.sincos);
 #pragma unroll
   for (int k = 0; k < 4; ++k)
     if (k < a.width - 1) X = fma(__ldg(t.coef + (int64_t)k * a.Nj + j), th[k], X);
-  double fl = 0.0;
-  if (a.noise_mode != JJA_NOISE_NONE) {
+  double x;
+  if (a.noise_mode == JJA_NOISE_NONE) {
+    x = Is.ptr ? X - view_at(Is, j, w) : X;   // (0 - Is) + X in the reference: the same rounding
+  } else {
     const double T = view_at(a.T, j, w);
     const double xi = a.noise_mode == JJA_NOISE_BUFFER ? a.noise[e] : philox_normal(a.seed, (uint64_t)e, (uint64_t)step);
-    fl = sqrt(2.0 * T * __ldg(t.Rv + j)) * xi;
+    const double fl = sqrt(2.0 * T * __ldg(t.Rv + j)) * xi;
+    x = (fl - view_at(Is, j, w)) + X;
   }
-  return ((fl - view_at(Is, j, w)) + X) * __ldg(t.inv_c0 + j);
+  return x * __ldg(t.inv_c0 + j);
 }
 
 // q for the first step of a run, from the stored phase history
@@ -200,13 +230,16 @@ __global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const do
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NfW; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = e / a.W, w = e - p * a.W;
     double acc = 0.0;
-    for (int64_t i = __ldg(t.fj_ptr + p); i < __ldg(t.fj_ptr + p + 1); ++i) {
-      const int64_t j = __ldg(t.fj_col + i);
+    const int64_t i0 = __ldg(t.fj_ptr + p), i1 = __ldg(t.fj_ptr + p + 1);
+    for (int64_t i = i0; i < i1; ++i) {
+      const int code = __ldg(t.fj_col + i);          // (junction << 1) | (A entry is -1)
+      const int64_t j = code >> 1;
       double v = q[j * a.W + w];
       if (a.theta_s) v -= a.theta_s[j * a.W + w];
-      acc = fma(__ldg(t.fj_val + i), v, acc);
+      v = signed_by(v, code & 1);
+      acc = (i == i0) ? v : acc + v;
     }
-    if (a.f.ptr) acc -= kTwoPi * view_at(a.f, __ldg(t.face_orig + p), w);
+    if (a.f.ptr) acc = fma(-kTwoPi, view_at(a.f, __ldg(t.face_orig + p), w), acc);
     b[e] = acc;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *a.d_step += 1;
@@ -222,12 +255,10 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, Tables t, double* __
   const int64_t next_step = *a.d_step;   // already advanced by k_face_rhs
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = e / a.W, w = e - j * a.W;
-    double y = 0.0;
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-      const int p = __ldg(t.jf_face + 2 * j + i);
-      if (p >= 0) y = fma(__ldg(t.jf_val + 2 * j + i), J[(int64_t)p * a.W + w], y);
-    }
+    // y = A^T J: a junction lies on one or two faces; the +-1 entries are sign flips
+    const int p0 = __ldg(t.jf_face + 2 * j), p1 = __ldg(t.jf_face + 2 * j + 1);
+    double y = p0 >= 0 ? signed_by(J[(int64_t)(p0 >> 1) * a.W + w], p0 & 1) : 0.0;
+    if (p1 >= 0) y += signed_by(J[(int64_t)(p1 >> 1) * a.W + w], p1 & 1);
     const double th = fma(y, __ldg(t.inv_c0 + j), -q[e]);
     double hist[4];
     if (kFuseNext) {
@@ -617,22 +648,22 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     const int Nj = d->Nj, Nf = d->Nf;
     // face -> junction entries in the factor's face order; junction -> (<= 2) faces
     std::vector<int64_t> fj_ptr(Nf + 1, 0);
-    std::vector<int32_t> fj_col;
-    std::vector<double> fj_val;
-    std::vector<int32_t> face_orig(Nf), jf_face(2 * (size_t)Nj, -1);
-    std::vector<double> jf_val(2 * (size_t)Nj, 0.0);
+    std::vector<int32_t> fj_col;                 // (junction << 1) | (entry is -1)
+    std::vector<int32_t> face_orig(Nf), jf_face(2 * (size_t)Nj, -1);   // (face << 1) | (entry is -1)
     for (int pn = 0; pn < Nf; ++pn) {
       const int f = F.perm[pn];
       face_orig[pn] = f;
       for (int64_t q = d->a_rowptr[f]; q < d->a_rowptr[f + 1]; ++q) {
         const int j = d->a_col[q];
+        const double v = d->a_val[q];
         if (j < 0 || j >= Nj) throw Error(JJA_ERR_ARG, "cycle matrix column out of range");
-        fj_col.push_back(j);
-        fj_val.push_back(d->a_val[q]);
+        if (v != 1.0 && v != -1.0) throw Error(JJA_ERR_ARG, "cycle matrix entries must be +1 or -1");
+        if (Nj >= (1 << 30) || Nf >= (1 << 30)) throw Error(JJA_ERR_ARG, "too many junctions or faces");
+        const int neg = v < 0 ? 1 : 0;
+        fj_col.push_back((j << 1) | neg);
         int slot = jf_face[2 * (size_t)j] < 0 ? 0 : (jf_face[2 * (size_t)j + 1] < 0 ? 1 : -1);
         if (slot < 0) throw Error(JJA_ERR_ARG, "a junction lies on more than two faces (non-planar cycle matrix)");
-        jf_face[2 * (size_t)j + slot] = pn;
-        jf_val[2 * (size_t)j + slot] = d->a_val[q];
+        jf_face[2 * (size_t)j + slot] = (pn << 1) | neg;
       }
       fj_ptr[pn + 1] = (int64_t)fj_col.size();
     }
@@ -642,22 +673,29 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->t.Rv = p->up(d->Rv, Nj);
     p->t.fj_ptr = p->up(fj_ptr.data(), fj_ptr.size());
     p->t.fj_col = p->up(fj_col.data(), fj_col.size());
-    p->t.fj_val = p->up(fj_val.data(), fj_val.size());
     p->t.face_orig = p->up(face_orig.data(), face_orig.size());
     p->t.jf_face = p->up(jf_face.data(), jf_face.size());
-    p->t.jf_val = p->up(jf_val.data(), jf_val.size());
     p->perm = p->up(F.perm.data(), F.perm.size());
     {
       // sin/cos of k pi/2048: first-quadrant values in extended precision, rounded once to
-      // double, then exact quadrant symmetries, so sin(m pi) and cos(m pi + pi/2) are exactly 0
-      std::vector<double2> tab(kSinTable);
+      // double, then exact quadrant symmetries, so sin(m pi) and cos(m pi + pi/2) are exactly 0.
+      // Entry k: {S, C}, {-S/2, float S | float C << 32}.
+      std::vector<double2> tab(2 * (size_t)kSinTable);
       const long double pi_l = 3.141592653589793238462643383279502884L;
       for (int k = 0; k < kSinTable; ++k) {
         const int q = k / 1024, r = k % 1024;
         const long double ang = (long double)r * pi_l / 2048.0L;
         const double s0 = (double)sinl(ang), c0 = (double)cosl(ang);
         const double sv[4] = {s0, c0, -s0, -c0}, cv[4] = {c0, -s0, -c0, s0};
-        tab[k] = make_double2(sv[q], cv[q]);
+        const float sf = (float)sv[q], cf = (float)cv[q];
+        uint32_t sb, cb;
+        std::memcpy(&sb, &sf, 4);
+        std::memcpy(&cb, &cf, 4);
+        const uint64_t packed = (uint64_t)sb | ((uint64_t)cb << 32);
+        double pd;
+        std::memcpy(&pd, &packed, 8);
+        tab[2 * (size_t)k] = make_double2(sv[q], cv[q]);
+        tab[2 * (size_t)k + 1] = make_double2(-0.5 * sv[q], pd);
       }
       p->t.sincos = p->up(tab.data(), tab.size());
     }
