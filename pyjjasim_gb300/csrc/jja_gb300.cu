@@ -275,9 +275,40 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, Tables t, double* __
 }
 
 // ------------------------------------------------------------------------------------------
-// supernodal triangular solves. Work item = (supernode s, rows [r0, r1), problems [w0, w0+WB)).
+// supernodal triangular solves. Work item = (supernode s, output rows [r0, r1), problems
+// [w0, w0+WB), contraction range [c_lo, c_hi)), packed in an int4:
+//   x = s, y = r0 | r1 << 16, z = w0 | partial << 30, w = c_lo | c_hi << 16.
 // Lane l handles problem w0 + l % WB and rows r0 + l / WB + t * (32 / WB), t < kRowsPerLane.
+// Levels with few items split long dot products over several items ("partial" items add
+// their share atomically into outputs that were zeroed at the start of the solve), so the
+// top of the elimination tree has enough warps in flight to hide L2 latency.
 // ------------------------------------------------------------------------------------------
+struct Item {
+  int s, r0, r1, w0, c_lo, c_hi;
+  bool partial;
+};
+
+__device__ __forceinline__ Item unpack_item(int4 v) {
+  Item it;
+  it.s = v.x;
+  it.r0 = v.y & 0xffff;
+  it.r1 = (int)((unsigned)v.y >> 16);
+  it.w0 = v.z & 0x3fffffff;
+  it.partial = (v.z >> 30) & 1;
+  it.c_lo = v.w & 0xffff;
+  it.c_hi = (int)((unsigned)v.w >> 16);
+  return it;
+}
+
+// zero the listed rows of an (Nf x W) vector before a sweep whose partial items accumulate there
+__global__ void k_zero_rows(double* __restrict__ v, const int32_t* __restrict__ rows, int n_rows, int W) {
+  const int64_t n = (int64_t)n_rows * W;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / W, w = e - i * W;
+    v[(int64_t)__ldg(rows + i) * W + w] = 0.0;
+  }
+}
+
 struct FactorDev {
   const int32_t* col0;
   const int32_t* k;
@@ -295,8 +326,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, 
   const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (it >= n_items) return;
   const int lane = threadIdx.x & 31;
-  const int4 item = items[it];
-  const int s = item.x, r0 = item.y, r1 = item.z, w0 = item.w;
+  const Item item = unpack_item(items[it]);
+  const int s = item.s, r0 = item.r0, r1 = item.r1, w0 = item.w0;
   const int LG = 32 / WB;
   const int w = w0 + lane % WB;
   if (w >= W) return;
@@ -313,8 +344,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, 
   }
   // dot products over the supernode's columns; loads of kUnroll columns are issued before
   // their FMAs so a warp keeps several L2 requests in flight (top levels have few warps)
-  const int jend = min(k, r1);
-  int j = 0;
+  const int jend = min(min(k, r1), item.c_hi);
+  int j = item.c_lo;
   for (; j + kUnroll <= jend; j += kUnroll) {
     double bj[kUnroll], fv[kUnroll][kRowsPerLane];
 #pragma unroll
@@ -339,8 +370,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, 
   for (int t = 0; t < kRowsPerLane; ++t) {
     const int r = r0 + rl + t * LG;
     if (r >= r1) break;
-    if (r < k) z[(int64_t)(c0 + r) * W + w] = acc[t];
-    else atomicAdd(b + (int64_t)__ldg(R + (r - k)) * W + w, -acc[t]);
+    if (r >= k) atomicAdd(b + (int64_t)__ldg(R + (r - k)) * W + w, -acc[t]);
+    else if (item.partial) atomicAdd(z + (int64_t)(c0 + r) * W + w, acc[t]);
+    else z[(int64_t)(c0 + r) * W + w] = acc[t];
   }
   (void)m;
 }
@@ -351,14 +383,17 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
   const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (it >= n_items) return;
   const int lane = threadIdx.x & 31;
-  const int4 item = items[it];
-  const int s = item.x, i0 = item.y, i1 = item.z, w0 = item.w;
+  const Item item = unpack_item(items[it]);
+  const int s = item.s, i0 = item.r0, i1 = item.r1, w0 = item.w0;
   const int LG = 32 / WB;
   const int w = w0 + lane % WB;
   if (w >= W) return;
   const int rl = lane / WB;
   const int c0 = __ldg(F.col0 + s), k = __ldg(F.k + s), m = __ldg(F.m + s);
   const double* Fs = F.frow + __ldg(F.valptr + s);
+  // contraction rows [c_lo, c_hi) of [i0, k + m): diagonal part r < k, off-diagonal part r >= k
+  const int r_diag_end = min(k, item.c_hi);
+  const int q_begin = max(item.c_lo, k) - k, q_end = max(item.c_hi, k) - k;
   double acc[kRowsPerLane];
   int ii[kRowsPerLane];
 #pragma unroll
@@ -368,8 +403,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
     ii[t] = i < i1 ? i : i0;
   }
   // diagonal block: inv(L11)^T z_s (zero above the diagonal, so start at row i0)
-  int r = i0;
-  for (; r + kUnroll <= k; r += kUnroll) {
+  int r = max(i0, item.c_lo);
+  for (; r + kUnroll <= r_diag_end; r += kUnroll) {
     double zr[kUnroll], fv[kUnroll][kRowsPerLane];
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) zr[u] = __ldg(z + (int64_t)(c0 + r + u) * W + w);
@@ -382,7 +417,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
 #pragma unroll
       for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(fv[u][t], zr[u], acc[t]);
   }
-  for (; r < k; ++r) {
+  for (; r < r_diag_end; ++r) {
     const double zr = __ldg(z + (int64_t)(c0 + r) * W + w);
     const double* row = Fs + (int64_t)r * k;
 #pragma unroll
@@ -390,8 +425,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
   }
   // off-diagonal rows: - (L21 inv(L11))^T x[R_s]; index loads, then value loads, then FMAs
   const int32_t* R = F.rows + __ldg(F.rowptr + s);
-  int q = 0;
-  for (; q + kUnroll <= m; q += kUnroll) {
+  int q = q_begin;
+  for (; q + kUnroll <= q_end; q += kUnroll) {
     int idx[kUnroll];
     double xr[kUnroll], fv[kUnroll][kRowsPerLane];
 #pragma unroll
@@ -407,7 +442,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
 #pragma unroll
       for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(-fv[u][t], xr[u], acc[t]);
   }
-  for (; q < m; ++q) {
+  for (; q < q_end; ++q) {
     const double xr = x[(int64_t)__ldg(R + q) * W + w];
     const double* row = Fs + (int64_t)(k + q) * k;
 #pragma unroll
@@ -417,8 +452,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
   for (int t = 0; t < kRowsPerLane; ++t) {
     const int i = i0 + rl + t * LG;
     if (i >= i1) break;
-    x[(int64_t)(c0 + i) * W + w] = acc[t];
+    if (item.partial) atomicAdd(x + (int64_t)(c0 + i) * W + w, acc[t]);
+    else x[(int64_t)(c0 + i) * W + w] = acc[t];
   }
+  (void)m;
 }
 
 __global__ void k_eval_sin(const double* __restrict__ x, double* __restrict__ out, int64_t n,
@@ -471,6 +508,9 @@ struct jja_plan {
   double *b = nullptr, *z = nullptr, *x = nullptr, *xj = nullptr;
   int32_t* perm = nullptr;   // new -> old face
   int64_t* d_step = nullptr;
+  int32_t* zrows_f = nullptr;   // rows of z accumulated by partial forward items
+  int32_t* zrows_b = nullptr;   // rows of x accumulated by partial backward items
+  int nz_f = 0, nz_b = 0;
   int64_t bytes = 0;
   // cached graph of a fixed-length step sequence
   cudaGraphExec_t gexec = nullptr;
@@ -490,7 +530,16 @@ struct jja_plan {
 
 namespace {
 
+// zero the rows that partial items of the coming sweep accumulate into
+void launch_zero_rows(jja_plan* p, cudaStream_t st, bool forward, double* v) {
+  const int n = forward ? p->nz_f : p->nz_b;
+  if (!n) return;
+  k_zero_rows<<<grid_for((int64_t)n * p->W, 256), 256, 0, st>>>(v, forward ? p->zrows_f : p->zrows_b, n, p->W);
+  g_launches++;
+}
+
 void launch_levels(jja_plan* p, cudaStream_t st, bool forward) {
+  launch_zero_rows(p, st, forward, forward ? p->z : p->x);
   if (forward) {  // levels ascending (children before parents); b is consumed, z produced
     for (int l = 0; l < p->n_levels; ++l) {
       const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
@@ -721,22 +770,68 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->n_levels = F.n_levels;
     std::vector<std::vector<int>> by_level(F.n_levels);
     for (int s = 0; s < F.ns; ++s) by_level[F.sn_level[s]].push_back(s);
+    if (d->W >= (1 << 30)) throw Error(JJA_ERR_ARG, "jja_plan_create: W too large");
+    for (int s = 0; s < F.ns; ++s)
+      if (F.sn_k[s] + F.sn_m[s] >= 65536) throw Error(JJA_ERR_ARG, "jja_plan_create: supernode with >= 65536 rows");
+    auto pack = [](int s, int r0, int r1, int w0, bool partial, int c_lo, int c_hi) {
+      return make_int4(s, r0 | (r1 << 16), w0 | ((int)partial << 30), c_lo | (c_hi << 16));
+    };
+    // Levels with fewer items than can fill the GPU split each dot product into pieces of at
+    // least kMinPiece terms (multiples of the unroll), enough to reach kTargetItems warps.
+    constexpr int kTargetItems = 152 * 24;
+    constexpr int kMinPiece = 16;
+    const int nwc = (d->W + WB - 1) / WB;
+    auto pieces_of = [&](int len, int split) {
+      const int np = std::max(1, std::min(split, len / kMinPiece));
+      const int plen = ((len + np - 1) / np + kUnroll - 1) / kUnroll * kUnroll;
+      return std::max(plen, 1);
+    };
     std::vector<int4> fi, bi;
+    std::vector<int32_t> zf, zb;   // rows of z / x that partial items accumulate into
     p->fwd_ptr.assign(1, 0);
     p->bwd_ptr.assign(1, 0);
     for (int l = 0; l < F.n_levels; ++l) {
+      int64_t nfw = 0, nbw = 0;
       for (int s : by_level[l]) {
         const int k = F.sn_k[s], nf = k + F.sn_m[s];
-        for (int r0 = 0; r0 < nf; r0 += RPI)
-          for (int w0 = 0; w0 < d->W; w0 += WB) fi.push_back(make_int4(s, r0, std::min(nf, r0 + RPI), w0));
-        for (int i0 = 0; i0 < k; i0 += RPI)
-          for (int w0 = 0; w0 < d->W; w0 += WB) bi.push_back(make_int4(s, i0, std::min(k, i0 + RPI), w0));
+        nfw += (int64_t)((nf + RPI - 1) / RPI) * nwc;
+        nbw += (int64_t)((k + RPI - 1) / RPI) * nwc;
+      }
+      const int fsplit = (int)std::max<int64_t>(1, (kTargetItems + nfw - 1) / std::max<int64_t>(nfw, 1));
+      const int bsplit = (int)std::max<int64_t>(1, (kTargetItems + nbw - 1) / std::max<int64_t>(nbw, 1));
+      for (int s : by_level[l]) {
+        const int k = F.sn_k[s], nf = k + F.sn_m[s], c0 = F.sn_col0[s];
+        bool zf_s = false, zb_s = false;
+        const int fplen = pieces_of(k, fsplit);
+        for (int r0 = 0; r0 < nf; r0 += RPI) {
+          const int r1 = std::min(nf, r0 + RPI), jmax = std::min(k, r1);
+          const bool partial = jmax > fplen;
+          zf_s |= partial && r0 < k;
+          for (int c_lo = 0; c_lo < jmax; c_lo += fplen)
+            for (int w0 = 0; w0 < d->W; w0 += WB)
+              fi.push_back(pack(s, r0, r1, w0, partial, c_lo, std::min(jmax, c_lo + fplen)));
+        }
+        for (int i0 = 0; i0 < k; i0 += RPI) {
+          const int i1 = std::min(k, i0 + RPI), len = nf - i0;
+          const int bplen = pieces_of(len, bsplit);
+          const bool partial = len > bplen;
+          zb_s |= partial;
+          for (int c_lo = i0; c_lo < nf; c_lo += bplen)
+            for (int w0 = 0; w0 < d->W; w0 += WB)
+              bi.push_back(pack(s, i0, i1, w0, partial, c_lo, std::min(nf, c_lo + bplen)));
+        }
+        if (zf_s) for (int i = 0; i < k; ++i) zf.push_back(c0 + i);
+        if (zb_s) for (int i = 0; i < k; ++i) zb.push_back(c0 + i);
       }
       p->fwd_ptr.push_back((int64_t)fi.size());
       p->bwd_ptr.push_back((int64_t)bi.size());
     }
     p->fwd_items = p->up(fi.data(), fi.size());
     p->bwd_items = p->up(bi.data(), bi.size());
+    p->nz_f = (int)zf.size();
+    p->nz_b = (int)zb.size();
+    p->zrows_f = p->up(zf.data(), zf.size());
+    p->zrows_b = p->up(zb.data(), zb.size());
     const size_t NfW = (size_t)Nf * d->W, NjW = (size_t)Nj * d->W;
     p->b = p->up<double>(nullptr, NfW);
     p->z = p->up<double>(nullptr, NfW);
@@ -800,6 +895,7 @@ double* static_scratch_for_current_device() {
 
 // the level sweeps of launch_levels with explicit work vectors
 void launch_levels_into(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x) {
+  launch_zero_rows(p, st, forward, forward ? z : x);
   if (forward) {
     for (int l = 0; l < p->n_levels; ++l) {
       const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
