@@ -55,6 +55,12 @@ def bias_slice(rank, world, W=W_BATCH):
     return allb[rank * W:(rank + 1) * W]
 
 
+def factor_opts(args):
+    """Factorisation options from the command line (ordering, supernode amalgamation)."""
+    z, f = args.relax.split(",")
+    return {"ordering": args.ordering, "relax": (int(z), float(f))}
+
+
 def make_problem(mod, Nt, bias, store_last=True, W=None):
     a = mod.SquareArray(NX, NY)
     Is = a.current_base(0.0)[:, None, None] * np.asarray(bias)[None, :, None]
@@ -214,7 +220,7 @@ def profile_mode(args):
     from pyjjasim_gb300.backend import GpuSimulation
     torch.cuda.set_device(0)
     prob = make_problem(G, 1, np.linspace(0.0, 2.0, args.W))
-    sim = GpuSimulation(prob)
+    sim = GpuSimulation(prob, **factor_opts(args))
     sim.run(3, use_graph=False)
     sim.synchronize()
     t0 = time.perf_counter()
@@ -238,6 +244,8 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling mode: plan, 3 eager warm-up steps, then this many eager steps, nothing else")
     ap.add_argument("--W", type=int, default=W_BATCH, help="problems per launch (profiling mode)")
+    ap.add_argument("--ordering", default="nd", choices=["nd", "mmd"], help="fill-reducing order of the factor")
+    ap.add_argument("--relax", default="-1,-1", help="supernode amalgamation: max zeros,max fraction (-1: default)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -264,7 +272,7 @@ def main():
     Nj, Nf, W = prob.get_circuit()._Nj(), prob.get_circuit()._Nf(), prob.get_problem_count()
 
     t0 = time.perf_counter()
-    sim = GpuSimulation(prob)
+    sim = GpuSimulation(prob, **factor_opts(args))
     sim.synchronize()
     t_plan = time.perf_counter() - t0
     fstats = None
@@ -347,7 +355,7 @@ def main():
             "stage_share": stage_share}
         # plain GPU path: one problem per launch
         prob1 = make_problem(G, 1, [1.0])
-        sim1 = GpuSimulation(prob1)
+        sim1 = GpuSimulation(prob1, **factor_opts(args))
         sim1.run(max(args.warmup, 40), use_graph=True)
         sim1.synchronize()
         k1 = max(args.steps, 200)
@@ -364,10 +372,10 @@ def main():
         # end to end through the public API with host buffers
         if not args.no_e2e:
             pe = make_problem(G, args.steps, bias)
-            pe.compute()                                  # warm: plan cache, graph capture
+            pe.compute(**factor_opts(args))               # warm: plan cache, graph capture
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            res = pe.compute()
+            res = pe.compute(**factor_opts(args))
             th = res.get_theta()
             t_e2e = time.perf_counter() - t0
             assert np.isfinite(th).all()

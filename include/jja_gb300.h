@@ -42,7 +42,7 @@ typedef struct {
   int keep_factor;    /* keep plain Cholesky columns for host checks */
   int relax_zeros;    /* merge a child supernode into its parent if that adds <= this many zeros */
   double relax_frac;  /* ... or <= this fraction of the merged block (both 0: fundamental only;
-                         negative values select the defaults 64 and 0.1) */
+                         negative values select the defaults 16 and 0.05) */
 } jja_factor_opts;
 
 typedef struct {

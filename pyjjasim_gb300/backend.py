@@ -111,7 +111,8 @@ class GpuSimulation:
     ``run_timed`` advances with per-stage CUDA-event timing, ``theta`` returns the newest phase.
     """
 
-    def __init__(self, problem, noise="philox", seed=None, device=None, nd_leaf=8, stream=None):
+    def __init__(self, problem, noise="philox", seed=None, device=None, nd_leaf=8, stream=None, ordering="nd",
+                 relax=(-1, -1.0)):
         torch = self.torch = _torch()
         c = problem.get_circuit()
         if not _is_default_cpr(problem.get_current_phase_relation()):
@@ -123,7 +124,8 @@ class GpuSimulation:
         self.h2d_bytes = 0
         with torch.cuda.device(self.dev):
             self.stream = stream if stream is not None else torch.cuda.Stream(device=self.dev)
-            self.plan = P.get_plan(c, problem._dt(), self.W, self.width, problem.stencil, nd_leaf=nd_leaf)
+            self.plan = P.get_plan(c, problem._dt(), self.W, self.width, problem.stencil, nd_leaf=nd_leaf,
+                                   ordering=ordering, relax=relax)
             hist0 = [problem.config_at_minus_1, problem.config_at_minus_2]
             if self.width >= 4:
                 hist0.append(problem.config_at_minus_3)
@@ -228,9 +230,13 @@ class GpuSimulation:
 
 
 def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", seed=None, device=None,
-                        use_graph=True, nd_leaf=8, stream=None):
-    """GPU time-stepping core; see the module docstring for the contract."""
-    sim = GpuSimulation(problem, noise=noise, seed=seed, device=device, nd_leaf=nd_leaf, stream=stream)
+                        use_graph=True, nd_leaf=8, stream=None, ordering="nd", relax=(-1, -1.0)):
+    """GPU time-stepping core; see the module docstring for the contract.
+
+    ``ordering`` ("nd" or "mmd") and ``relax`` ((max zeros, max fraction) of supernode
+    amalgamation; negative = library defaults) select how the face-space matrix is factorised."""
+    sim = GpuSimulation(problem, noise=noise, seed=seed, device=device, nd_leaf=nd_leaf, stream=stream,
+                        ordering=ordering, relax=relax)
     torch = sim.torch
     Nj, W, Nt, width = sim.Nj, sim.W, problem._Nt(), sim.width
     th_store_mask = np.asarray(th_store_mask, bool)

@@ -106,13 +106,15 @@ struct StepArgs {
   double* I_out;
   double e[4];
   double dt;
+  jja_view Isq;        // Is / c0 (plan-owned buffer refreshed at the start of a run)
+  int resistive;       // width 3 and no capacitance anywhere: c1 / c0 = -1, c2 = 0
 };
 
 struct Tables {
-  const double* Ic;
+  const double* Icq;    // Ic / c0
   const double* inv_c0;
-  const double* coef;   // (width-1) x Nj
-  const double* Rv;
+  const double* coefq;  // (width-1) x Nj: c_k / c0
+  const double* Rvq;    // Rv / c0^2 (noise amplitude over c0 is sqrt(2 T Rvq))
   const int64_t* fj_ptr;   // permuted face -> junction entries
   const int32_t* fj_col;
   const int32_t* face_orig;
@@ -182,8 +184,11 @@ __device__ __forceinline__ double fast_sin(double x, const double2* __restrict__
 
 // q(j, w) = x / c0 for the step whose phase history is th[0..] (time_evolution.py:533-558):
 //   x = sqrt(2 T Rv) xi - Is + Ic sin(sum_k e_k th_k) + sum_k c_k th_k
+// evaluated with the coefficients already divided by c0 (Icq = Ic/c0, coefq_k = c_k/c0,
+// Rvq = Rv/c0^2, Isq = Is/c0), which saves the final multiply. Without capacitance
+// (stencil width 3) c1/c0 = -1 and c2 = 0 exactly, so x/c0 = Icq sin - th1 - Isq.
 __device__ __forceinline__ double junction_q(const StepArgs& a, const Tables& t, int64_t e, int64_t j, int64_t w,
-                                            const double* th, const jja_view& Is, int64_t step) {
+                                            const double* th, int64_t step) {
   double arg;
   if (a.width == 3) {
     arg = fma(2.0, th[0], -th[1]);        // 2 th1 - th2 with the reference's single rounding
@@ -193,20 +198,32 @@ __device__ __forceinline__ double junction_q(const StepArgs& a, const Tables& t,
     for (int k = 1; k < 4; ++k)
       if (k < a.width - 1) arg = fma(a.e[k], th[k], arg);
   }
-  double X = __ldg(t.Ic + j) * fast_sin(arg, t.sincos);
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-    if (k < a.width - 1) X = fma(__ldg(t.coef + (int64_t)k * a.Nj + j), th[k], X);
-  double x;
-  if (a.noise_mode == JJA_NOISE_NONE) {
-    x = Is.ptr ? X - view_at(Is, j, w) : X;   // (0 - Is) + X in the reference: the same rounding
+  const double s = fast_sin(arg, t.sincos);
+  double X;
+  if (a.resistive) {
+    X = fma(__ldg(t.Icq + j), s, -th[0]);
   } else {
-    const double T = view_at(a.T, j, w);
-    const double xi = a.noise_mode == JJA_NOISE_BUFFER ? a.noise[e] : philox_normal(a.seed, (uint64_t)e, (uint64_t)step);
-    const double fl = sqrt(2.0 * T * __ldg(t.Rv + j)) * xi;
-    x = (fl - view_at(Is, j, w)) + X;
+    X = __ldg(t.Icq + j) * s;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k < a.width - 1) X = fma(__ldg(t.coefq + (int64_t)k * a.Nj + j), th[k], X);
   }
-  return x * __ldg(t.inv_c0 + j);
+  if (a.noise_mode == JJA_NOISE_NONE)
+    return a.Isq.ptr ? X - view_at(a.Isq, j, w) : X;   // (0 - Is) + X in the reference
+  const double T = view_at(a.T, j, w);
+  const double xi = a.noise_mode == JJA_NOISE_BUFFER ? a.noise[e] : philox_normal(a.seed, (uint64_t)e, (uint64_t)step);
+  const double fl = sqrt(2.0 * T * __ldg(t.Rvq + j)) * xi;
+  return (fl - view_at(a.Isq, j, w)) + X;
+}
+
+// Isq = Is / c0 per junction, refreshed at the start of every run (and every host-driven step)
+__global__ void __launch_bounds__(256) k_scale_sources(jja_view Is, const double* __restrict__ inv_c0,
+                                                       double* __restrict__ Isq, int Nj, int W) {
+  const int64_t NjW = (int64_t)Nj * W;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = e / W, w = e - j * W;
+    Isq[e] = view_at(Is, j, w) * __ldg(inv_c0 + j);
+  }
 }
 
 // q for the first step of a run, from the stored phase history
@@ -218,7 +235,7 @@ __global__ void __launch_bounds__(256) k_junction(StepArgs a, Tables t, double* 
     double th[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) th[k] = (k < a.width - 1) ? a.h[k][e] : 0.0;
-    q[e] = junction_q(a, t, e, j, w, th, a.Is, step);
+    q[e] = junction_q(a, t, e, j, w, th, step);
   }
 }
 
@@ -270,7 +287,7 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, Tables t, double* __
     if (a.th_out && a.th_slot >= 0) a.th_out[a.th_slot * NjW + e] = th;
     if (a.I_out && a.I_slot >= 0) a.I_out[a.I_slot * NjW + e] = y + view_at(a.Is, j, w);
     if (a.theta_s && a.Vs.ptr) a.theta_s[e] += view_at(a.Vs, j, w) * a.dt;
-    if (kFuseNext) q[e] = junction_q(a, t, e, j, w, hist, a.Is, next_step);
+    if (kFuseNext) q[e] = junction_q(a, t, e, j, w, hist, next_step);
   }
 }
 
@@ -508,6 +525,8 @@ struct jja_plan {
   double *b = nullptr, *z = nullptr, *x = nullptr, *xj = nullptr;
   int32_t* perm = nullptr;   // new -> old face
   int64_t* d_step = nullptr;
+  double* isq = nullptr;        // Is / c0 (Nj x W)
+  int resistive = 0;
   int32_t* zrows_f = nullptr;   // rows of z accumulated by partial forward items
   int32_t* zrows_b = nullptr;   // rows of x accumulated by partial backward items
   int nz_f = 0, nz_b = 0;
@@ -596,7 +615,16 @@ StepArgs make_args(jja_plan* p, jja_state* s) {
   a.th_out = s->th_out;
   a.I_out = s->I_out;
   a.dt = p->dt;
+  a.Isq = s->Is.ptr ? jja_view{p->isq, p->W, 1} : jja_view{nullptr, 0, 0};
+  a.resistive = p->resistive;
   return a;
+}
+
+// refresh Is / c0 from the state's current-source view (before the first step of a run)
+void launch_scale_sources(jja_plan* p, jja_state* s, cudaStream_t st) {
+  if (!s->Is.ptr) return;
+  k_scale_sources<<<grid_for((int64_t)p->Nj * p->W, 256), 256, 0, st>>>(s->Is, p->t.inv_c0, p->isq, p->Nj, p->W);
+  g_launches++;
 }
 
 // rotate the history: the oldest buffer receives theta_next
@@ -716,10 +744,26 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
       }
       fj_ptr[pn + 1] = (int64_t)fj_col.size();
     }
-    p->t.Ic = p->up(d->Ic, Nj);
+    {
+      // coefficients multiplied by 1/c0 once on the host (the junction kernels then need no
+      // final multiply). "resistive": width 3 and c2 = Cv = 0 everywhere, in which case
+      // c1 = -Rv - 2 Cv = -c0 exactly and c1/c0 = -1 (time_evolution.py:477-478, 489)
+      const int nk = d->stencil_width - 1;
+      std::vector<double> icq(Nj), coefq((size_t)nk * Nj), rvq(Nj);
+      bool resistive = d->stencil_width == 3;
+      for (int j = 0; j < Nj; ++j) {
+        const double ic0 = d->inv_c0[j];
+        icq[j] = d->Ic[j] * ic0;
+        rvq[j] = d->Rv[j] * ic0 * ic0;
+        for (int k = 0; k < nk; ++k) coefq[(size_t)k * Nj + j] = d->coef[(size_t)k * Nj + j] * ic0;
+        if (resistive) resistive = d->coef[(size_t)Nj + j] == 0.0;
+      }
+      p->resistive = resistive ? 1 : 0;
+      p->t.Icq = p->up(icq.data(), icq.size());
+      p->t.coefq = p->up(coefq.data(), coefq.size());
+      p->t.Rvq = p->up(rvq.data(), rvq.size());
+    }
     p->t.inv_c0 = p->up(d->inv_c0, Nj);
-    p->t.coef = p->up(d->coef, (size_t)(d->stencil_width - 1) * Nj);
-    p->t.Rv = p->up(d->Rv, Nj);
     p->t.fj_ptr = p->up(fj_ptr.data(), fj_ptr.size());
     p->t.fj_col = p->up(fj_col.data(), fj_col.size());
     p->t.face_orig = p->up(face_orig.data(), face_orig.size());
@@ -837,6 +881,7 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->z = p->up<double>(nullptr, NfW);
     p->x = p->up<double>(nullptr, NfW);
     p->xj = p->up<double>(nullptr, NjW);
+    p->isq = p->up<double>(nullptr, NjW);
     p->d_step = p->up<int64_t>(nullptr, 1);
     JJA_CUDA(cudaMemset(p->d_step, 0, sizeof(int64_t)));
     JJA_CUDA(cudaDeviceSynchronize());
@@ -961,6 +1006,7 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
     if (nsteps == 0) return;
     cudaStream_t st = (cudaStream_t)stream;
     JJA_CUDA(cudaMemcpyAsync(p->d_step, &s->step, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    launch_scale_sources(p, s, st);
     {
       StepArgs a = make_args(p, s);
       launch_junction(p, a, st);
@@ -1030,6 +1076,7 @@ int jja_run_timed(jja_plan* p, jja_state* s, int nsteps, double* stage_ms, void*
     std::vector<cudaEvent_t> ev(1 + 5 * (size_t)nsteps);
     for (auto& e : ev) JJA_CUDA(cudaEventCreate(&e));
     JJA_CUDA(cudaEventRecord(ev[0], st));
+    launch_scale_sources(p, s, st);
     {
       StepArgs a = make_args(p, s);
       launch_junction(p, a, st);

@@ -11,8 +11,8 @@ struct FactorOptions {
   int nd_leaf = 8;          // nested-dissection leaf size
   int max_supernode = 0;    // cap on supernode width (0 = none)
   int keep_factor = 0;      // keep the plain Cholesky columns (host checks only)
-  int relax_zeros = 64;     // amalgamate a child supernode when it adds at most this many zeros ...
-  double relax_frac = 0.1;  // ... or at most this fraction of the merged block's entries
+  int relax_zeros = 16;     // amalgamate a child supernode when it adds at most this many zeros ...
+  double relax_frac = 0.05; // ... or at most this fraction of the merged block's entries
 };
 
 // P K P^T = L L^T, stored per supernode as F_s = [inv(L11); L21 inv(L11)] ((k+m) x k,

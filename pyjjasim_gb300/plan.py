@@ -159,12 +159,27 @@ def _coords(circuit):
         return None
 
 
-def get_factor(circuit, dt, nd_leaf=8):
+def fill_reducing_order(K, ordering, circuit=None):
+    """(coords, perm) for HostFactor. "nd": the library's nested dissection on face centroids;
+    "mmd": the multiple-minimum-degree column order scipy's SuperLU computes on A + A^T
+    (less fill on 2D lattices, deeper elimination tree)."""
+    if ordering == "nd":
+        return (_coords(circuit) if circuit is not None else None), None
+    if ordering == "mmd":
+        import scipy.sparse.linalg
+        lu = scipy.sparse.linalg.splu(K.tocsc(), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.0,
+                                      options=dict(SymmetricMode=True))
+        return None, np.argsort(lu.perm_c).astype(np.int32)
+    raise ValueError(f"ordering must be 'nd' or 'mmd', not {ordering!r}")
+
+
+def get_factor(circuit, dt, nd_leaf=8, ordering="nd", relax=(-1, -1.0)):
     A, K = face_matrix(circuit, dt)
-    key = (_digest(K.indptr, K.indices, K.data), nd_leaf)
+    key = (_digest(K.indptr, K.indices, K.data), nd_leaf, ordering, tuple(relax))
     f = _FACTORS.get(key)
     if f is None:
-        f = HostFactor(K, coords=_coords(circuit), nd_leaf=nd_leaf)
+        coords, perm = fill_reducing_order(K, ordering, circuit)
+        f = HostFactor(K, coords=coords, perm=perm, nd_leaf=nd_leaf, relax_zeros=relax[0], relax_frac=relax[1])
         _FACTORS[key] = (f, A)
         while len(_FACTORS) > MAX_FACTORS:
             _FACTORS.popitem(last=False)
@@ -174,8 +189,8 @@ def get_factor(circuit, dt, nd_leaf=8):
     return _FACTORS[key][0], A, key
 
 
-def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=8):
-    factor, A, fkey = get_factor(circuit, dt, nd_leaf)
+def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=8, ordering="nd", relax=(-1, -1.0)):
+    factor, A, fkey = get_factor(circuit, dt, nd_leaf, ordering=ordering, relax=relax)
     Rv, Cv, coef = coefficients(circuit, dt, stencil)
     key = (fkey, W, stencil_width, _digest(np.asarray(circuit._Ic(), np.float64), *coef, Rv,
                                             A.indptr, A.indices, A.data))
