@@ -58,6 +58,7 @@ constexpr int kWarpsPerBlock = 4;   // level kernels: one warp per work item
 constexpr int kRowsPerLane = 4;     // rows of a work item handled by one lane
 constexpr int kUnroll = 4;          // columns whose loads are issued ahead of their FMAs
 constexpr double kTwoPi = 6.283185307179586;
+constexpr int kEllMax = 6;          // faces with up to 6 junctions (square 4, triangular 3, honeycomb 6)
 
 // ------------------------------------------------------------------------------------------
 // Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, "Parallel random
@@ -118,6 +119,8 @@ struct Tables {
   const int64_t* fj_ptr;   // permuted face -> junction entries
   const int32_t* fj_col;
   const int32_t* face_orig;
+  const int32_t* fj_ell;   // faces of <= kEllMax junctions: Nf x face_deg codes, padded with -1
+  int face_deg;            // 0 when some face has more than kEllMax junctions (CSR path)
   const int32_t* jf_face;  // 2 per junction: (permuted face << 1) | (A entry is -1), or -1
   const double2* sincos;   // per k < 4096: {S, C}, {-S/2, (float S, float C)}; S, C = sin, cos(k pi/2048)
 };
@@ -247,14 +250,32 @@ __global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const do
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NfW; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = e / a.W, w = e - p * a.W;
     double acc = 0.0;
-    const int64_t i0 = __ldg(t.fj_ptr + p), i1 = __ldg(t.fj_ptr + p + 1);
-    for (int64_t i = i0; i < i1; ++i) {
-      const int code = __ldg(t.fj_col + i);          // (junction << 1) | (A entry is -1)
-      const int64_t j = code >> 1;
-      double v = q[j * a.W + w];
-      if (a.theta_s) v -= a.theta_s[j * a.W + w];
-      v = signed_by(v, code & 1);
-      acc = (i == i0) ? v : acc + v;
+    if (t.face_deg) {
+      // fixed-degree layout: all index loads, then all value loads, then the sum
+      int code[kEllMax];
+      double v[kEllMax];
+#pragma unroll
+      for (int d = 0; d < kEllMax; ++d) code[d] = d < t.face_deg ? __ldg(t.fj_ell + p * t.face_deg + d) : -1;
+#pragma unroll
+      for (int d = 0; d < kEllMax; ++d) {
+        const int64_t j = code[d] >> 1;
+        v[d] = code[d] >= 0 ? q[j * a.W + w] : 0.0;
+        if (a.theta_s && code[d] >= 0) v[d] -= a.theta_s[j * a.W + w];
+      }
+      acc = signed_by(v[0], code[0] & 1);
+#pragma unroll
+      for (int d = 1; d < kEllMax; ++d)
+        if (code[d] >= 0) acc += signed_by(v[d], code[d] & 1);
+    } else {
+      const int64_t i0 = __ldg(t.fj_ptr + p), i1 = __ldg(t.fj_ptr + p + 1);
+      for (int64_t i = i0; i < i1; ++i) {
+        const int code = __ldg(t.fj_col + i);          // (junction << 1) | (A entry is -1)
+        const int64_t j = code >> 1;
+        double v = q[j * a.W + w];
+        if (a.theta_s) v -= a.theta_s[j * a.W + w];
+        v = signed_by(v, code & 1);
+        acc = (i == i0) ? v : acc + v;
+      }
     }
     if (a.f.ptr) acc = fma(-kTwoPi, view_at(a.f, __ldg(t.face_orig + p), w), acc);
     b[e] = acc;
@@ -766,6 +787,17 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->t.inv_c0 = p->up(d->inv_c0, Nj);
     p->t.fj_ptr = p->up(fj_ptr.data(), fj_ptr.size());
     p->t.fj_col = p->up(fj_col.data(), fj_col.size());
+    {
+      int deg = 0;
+      for (int pn = 0; pn < Nf; ++pn) deg = std::max<int>(deg, (int)(fj_ptr[pn + 1] - fj_ptr[pn]));
+      if (deg >= 1 && deg <= kEllMax) {
+        std::vector<int32_t> ell((size_t)Nf * deg, -1);
+        for (int pn = 0; pn < Nf; ++pn)
+          for (int64_t i = fj_ptr[pn]; i < fj_ptr[pn + 1]; ++i) ell[(size_t)pn * deg + (i - fj_ptr[pn])] = fj_col[i];
+        p->t.fj_ell = p->up(ell.data(), ell.size());
+        p->t.face_deg = deg;
+      }
+    }
     p->t.face_orig = p->up(face_orig.data(), face_orig.size());
     p->t.jf_face = p->up(jf_face.data(), jf_face.size());
     p->perm = p->up(F.perm.data(), F.perm.size());
