@@ -92,6 +92,9 @@ typedef struct {
   const double* Rv;        /* 1 / (dt R), noise amplitude sqrt(2 T Rv) (time_evolution.py:537) */
   double extrap[4];        /* CPR argument weights on theta(t-1), theta(t-2), ... (:547-553) */
   double dt;
+  const double* Ic_w;      /* optional (Nj x W) critical currents per problem (replaces Ic): W
+                              disorder realisations share one face-space matrix, since K does not
+                              depend on Ic; NULL to use Ic for every problem */
 } jja_plan_desc;
 
 /* Uploads the circuit tables and the factor to the current CUDA device and allocates the
@@ -139,6 +142,34 @@ int jja_run(jja_plan* p, jja_state* st, int nsteps, const int64_t* th_slot, cons
  * face right-hand side, forward solve, backward solve, update; and [5] the whole run.
  * Used by the benchmark to attribute step time to kernels; same results as jja_run. */
 int jja_run_timed(jja_plan* p, jja_state* st, int nsteps, double* stage_ms, void* stream);
+
+/* ---------------------------------------------------------------------------- adjoint --- */
+/* No counterpart in the reference (which has no derivatives): backward-through-time steps of
+ * the width-3 update for gradients of a loss L = sum_n <G_n, theta_n>. With a_n = dL/dtheta_n
+ * and mu_n = Q a_n, Q = D A^T K^-1 A D - D (D = diag(1/c0)), one call computes, for step n,
+ *   a_n   = G_n + (2 Ic cos phi_{n+1} + c1) mu_{n+1} + (-Ic cos phi_{n+2} + c2) mu_{n+2}
+ *   mu_n  = Q a_n  (one face-space solve with the same factor; K is symmetric)
+ * and accumulates usum += D a_n, musum += mu_n, gIc += mu_n sin phi_n, phi_n = 2 th_{n-1} - th_{n-2}.
+ * Then dL/dIc = gIc, dL/dIs = -musum, dL/df = -2 pi K^-1 A usum (jja_adjoint_flux).
+ * All arrays are device (Nj x W) except G (a view, NULL ptr = 0). */
+typedef struct {
+  jja_view G;             /* direct loss weights at step n (Nj rows) */
+  const double* th_m1;    /* theta_{n-1} */
+  const double* th_m2;    /* theta_{n-2} */
+  const double* mu_p1;    /* mu_{n+1}, NULL past the last step */
+  const double* mu_p2;    /* mu_{n+2}, NULL past the last step */
+  const double* cos_p1;   /* cos(phi_{n+1}) written by the call for step n+1 */
+  const double* cos_p2;   /* cos(phi_{n+2}) */
+  double* mu_out;         /* mu_n */
+  double* cos_out;        /* cos(phi_n) */
+  double* usum;           /* accumulators, zero before the first (last-step) call */
+  double* musum;
+  double* gIc;
+} jja_adjoint_args;
+
+int jja_adjoint_step(jja_plan* p, const jja_adjoint_args* args, void* stream);
+/* gf (device Nf x W, original face order) = -2 pi K^{-1} A usum: the flux gradient. */
+int jja_adjoint_flux(jja_plan* p, const double* usum, double* gf, void* stream);
 
 /* Face-space solve on the device: x = K^{-1} b for W right-hand sides (device arrays
  * Nf x W, original face order). Exposed for tests of the triangular-solve kernels. */

@@ -32,7 +32,7 @@ class PlanDesc(ctypes.Structure):
     _fields_ = [("Nj", c_int), ("Nf", c_int), ("W", c_int), ("stencil_width", c_int),
                 ("a_rowptr", P_i64), ("a_col", P_i32), ("a_val", P_f64),
                 ("Ic", P_f64), ("inv_c0", P_f64), ("coef", P_f64), ("Rv", P_f64),
-                ("extrap", c_double * 4), ("dt", c_double)]
+                ("extrap", c_double * 4), ("dt", c_double), ("Ic_w", P_f64)]
 
 
 class View(ctypes.Structure):
@@ -43,6 +43,12 @@ class State(ctypes.Structure):
     _fields_ = [("hist", c_void_p * 4), ("theta_s", c_void_p), ("Is", View), ("f", View), ("Vs", View), ("T", View),
                 ("noise_mode", c_int), ("noise", c_void_p), ("seed", ctypes.c_uint64), ("step", c_int64),
                 ("th_out", c_void_p), ("I_out", c_void_p)]
+
+
+class AdjointArgs(ctypes.Structure):
+    _fields_ = [("G", View), ("th_m1", c_void_p), ("th_m2", c_void_p), ("mu_p1", c_void_p), ("mu_p2", c_void_p),
+                ("cos_p1", c_void_p), ("cos_p2", c_void_p), ("mu_out", c_void_p), ("cos_out", c_void_p),
+                ("usum", c_void_p), ("musum", c_void_p), ("gIc", c_void_p)]
 
 
 # exported symbol -> (restype, argtypes); every symbol of include/jja_gb300.h
@@ -61,6 +67,8 @@ SIGNATURES = {
     "jja_run_timed": (c_int, [c_void_p, ctypes.POINTER(State), c_int, P_f64, c_void_p]),
     "jja_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "jja_solve_static": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "jja_adjoint_step": (c_int, [c_void_p, ctypes.POINTER(AdjointArgs), c_void_p]),
+    "jja_adjoint_flux": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "jja_eval_sin": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
     "jja_last_error": (ctypes.c_char_p, []),
     "jja_launch_count": (c_int64, []),

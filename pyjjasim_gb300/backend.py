@@ -81,6 +81,8 @@ class _Source:
         v = np.broadcast_to(np.asarray(self.getter(i) if value is None else value, np.float64), (self.N, self.W))
         r, c = self.shape
         host = np.ascontiguousarray(v[:r, :c])
+        if not host.flags.writeable:      # a broadcast view: torch.from_numpy wants writable memory
+            host = host.copy()
         with self.torch.cuda.stream(self.stream):
             self.buf.copy_(self.torch.from_numpy(host))
         self.h2d_bytes += host.nbytes
@@ -112,7 +114,9 @@ class GpuSimulation:
     """
 
     def __init__(self, problem, noise="philox", seed=None, device=None, nd_leaf=8, stream=None, ordering="nd",
-                 relax=(-1, -1.0)):
+                 relax=(-1, -1.0), Ic=None):
+        """``Ic``: optional (Nj, W) critical currents per problem, replacing the circuit's
+        (problems then differ in Ic but share the face-space matrix, which does not depend on Ic)."""
         torch = self.torch = _torch()
         c = problem.get_circuit()
         if not _is_default_cpr(problem.get_current_phase_relation()):
@@ -125,7 +129,7 @@ class GpuSimulation:
         with torch.cuda.device(self.dev):
             self.stream = stream if stream is not None else torch.cuda.Stream(device=self.dev)
             self.plan = P.get_plan(c, problem._dt(), self.W, self.width, problem.stencil, nd_leaf=nd_leaf,
-                                   ordering=ordering, relax=relax)
+                                   ordering=ordering, relax=relax, Ic_w=Ic)
             hist0 = [problem.config_at_minus_1, problem.config_at_minus_2]
             if self.width >= 4:
                 hist0.append(problem.config_at_minus_3)
@@ -215,6 +219,18 @@ class GpuSimulation:
         return dict(zip(("first_junction", "face_rhs", "forward", "backward", "update_junction", "total"),
                         ms.tolist()))
 
+    def history(self):
+        """Device tensors of the phase history, newest first (theta(t-1), theta(t-2), ...)."""
+        by_ptr = {t.data_ptr(): t for t in self.hist}
+        return [by_ptr[self.state.hist[k]] for k in range(self.width - 1)]
+
+    def set_history(self, thetas, step):
+        """Restart from a saved history (newest first) at global step index ``step``."""
+        for dst, src in zip(self.history(), thetas):
+            with self.torch.cuda.stream(self.stream):
+                dst.copy_(src)
+        self.state.step = int(step)
+
     def theta_ptr(self):
         return self.state.hist[0]
 
@@ -230,13 +246,13 @@ class GpuSimulation:
 
 
 def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", seed=None, device=None,
-                        use_graph=True, nd_leaf=8, stream=None, ordering="nd", relax=(-1, -1.0)):
+                        use_graph=True, nd_leaf=8, stream=None, ordering="nd", relax=(-1, -1.0), Ic=None):
     """GPU time-stepping core; see the module docstring for the contract.
 
     ``ordering`` ("nd" or "mmd") and ``relax`` ((max zeros, max fraction) of supernode
     amalgamation; negative = library defaults) select how the face-space matrix is factorised."""
     sim = GpuSimulation(problem, noise=noise, seed=seed, device=device, nd_leaf=nd_leaf, stream=stream,
-                        ordering=ordering, relax=relax)
+                        ordering=ordering, relax=relax, Ic=Ic)
     torch = sim.torch
     Nj, W, Nt, width = sim.Nj, sim.W, problem._Nt(), sim.width
     th_store_mask = np.asarray(th_store_mask, bool)
@@ -252,7 +268,8 @@ def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", se
         if zero:
             I_buf[n_init - 1 - lag] = 0.0          # cp(0) = Ic sin 0
         else:
-            I_buf[n_init - 1 - lag] = problem._cp(np.broadcast_to(th, (Nj, W)))
+            th = np.broadcast_to(th, (Nj, W))
+            I_buf[n_init - 1 - lag] = problem._cp(th) if Ic is None else np.asarray(Ic) * np.sin(th)
     th_idx = np.where(th_store_mask, np.cumsum(th_store_mask) - 1, -1).astype(np.int64)
     I_idx = np.where(I_store_mask, np.cumsum(I_store_mask) - 1, -1).astype(np.int64)
     max_slots = max(1, _MAX_OUT_BYTES // (2 * Nj * W * 8))

@@ -112,9 +112,12 @@ struct StepArgs {
 };
 
 struct Tables {
-  const double* Icq;    // Ic / c0
+  const double* Icq;    // Ic / c0: Nj values, or Nj x W when critical currents differ per problem
+  const double* Ic;     // Ic, same layout (the adjoint needs it unscaled)
+  int ic_per_w;         // 1: Icq / Ic are (Nj x W)
   const double* inv_c0;
   const double* coefq;  // (width-1) x Nj: c_k / c0
+  const double* coef;   // (width-1) x Nj: c_k
   const double* Rvq;    // Rv / c0^2 (noise amplitude over c0 is sqrt(2 T Rvq))
   const int64_t* fj_ptr;   // permuted face -> junction entries
   const int32_t* fj_col;
@@ -185,6 +188,34 @@ __device__ __forceinline__ double fast_sin(double x, const double2* __restrict__
   return r + f64_from_f32(tail);
 }
 
+// sin and cos from one reduction: cos(a + t) = C - S t - C t^2/2 + S t^3/6 + C t^4/24 + O(t^5)
+__device__ __forceinline__ void fast_sincos(double x, const double2* __restrict__ tab, double& s_out, double& c_out) {
+  if ((__double2hiint(x) & 0x7fffffff) >= 0x41086A00) {
+    sincos(x, &s_out, &c_out);
+    return;
+  }
+  const double s = fma(x, kSinScale, kRoundMagic);
+  const int k = __double2loint(s) & (kSinTable - 1);
+  const double kd = s - kRoundMagic;
+  double t = fma(-kd, kSinC1, x);
+  t = fma(-kd, kSinC2, t);
+  t = fma(-kd, kSinC3, t);
+  const double2 sc = __ldg(tab + 2 * k);       // S, C
+  const double2 hv = __ldg(tab + 2 * k + 1);   // -S/2, packed float S and C
+  const double t2 = t * t;
+  double rs = fma(sc.y, t, sc.x);              // S + C t
+  rs = fma(hv.x, t2, rs);                      // - S t^2/2
+  double rc = fma(-sc.x, t, sc.y);             // C - S t
+  rc = fma(-0.5 * sc.y, t2, rc);               // - C t^2/2
+  const float sf = __int_as_float(__double2loint(hv.y)), cf = __int_as_float(__double2hiint(hv.y));
+  const float tf = f32_from_f64(t);
+  const float tf2 = tf * tf, tf3 = tf2 * tf, tf4 = tf2 * tf2;
+  const float ts = fmaf(sf * (1.0f / 24.0f), tf4, -(cf * (1.0f / 6.0f)) * tf3);
+  const float tc = fmaf(cf * (1.0f / 24.0f), tf4, (sf * (1.0f / 6.0f)) * tf3);
+  s_out = rs + f64_from_f32(ts);
+  c_out = rc + f64_from_f32(tc);
+}
+
 // q(j, w) = x / c0 for the step whose phase history is th[0..] (time_evolution.py:533-558):
 //   x = sqrt(2 T Rv) xi - Is + Ic sin(sum_k e_k th_k) + sum_k c_k th_k
 // evaluated with the coefficients already divided by c0 (Icq = Ic/c0, coefq_k = c_k/c0,
@@ -202,11 +233,12 @@ __device__ __forceinline__ double junction_q(const StepArgs& a, const Tables& t,
       if (k < a.width - 1) arg = fma(a.e[k], th[k], arg);
   }
   const double s = fast_sin(arg, t.sincos);
+  const double icq = __ldg(t.Icq + (t.ic_per_w ? e : j));
   double X;
   if (a.resistive) {
-    X = fma(__ldg(t.Icq + j), s, -th[0]);
+    X = fma(icq, s, -th[0]);
   } else {
-    X = __ldg(t.Icq + j) * s;
+    X = icq * s;
 #pragma unroll
     for (int k = 0; k < 4; ++k)
       if (k < a.width - 1) X = fma(__ldg(t.coefq + (int64_t)k * a.Nj + j), th[k], X);
@@ -496,6 +528,73 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
   (void)m;
 }
 
+// ------------------------------------------------------------------------------------------
+// Adjoint (backward through time) of the width-3 step theta_n = Q x_n + const, with
+// x_n = Ic sin(phi_n) + c1 th_{n-1} + c2 th_{n-2} - Is, phi_n = 2 th_{n-1} - th_{n-2},
+// Q = D A^T K^-1 A D - D, D = diag(1/c0) (symmetric, so Q^T = Q and one factor serves).
+// With a_n = dL/dtheta_n and mu_n = Q a_n:
+//   a_n = G_n + (2 Ic cos phi_{n+1} + c1) mu_{n+1} + (-Ic cos phi_{n+2} + c2) mu_{n+2}
+//   dL/dIc += mu_n sin phi_n,  dL/dIs = -sum mu_n,  dL/df = -2 pi K^-1 A D sum a_n.
+// A step is: k_adj_a (a_n -> u = D a_n), the face kernel (b = A u), the two triangular
+// sweeps (nu = K^-1 b), k_adj_mu (mu_n = D A^T nu - u, sin/cos phi_n, accumulations).
+// ------------------------------------------------------------------------------------------
+struct AdjArgs {
+  int Nj, W;
+  jja_view G;
+  const double* th_m1;
+  const double* th_m2;
+  const double* mu_p1;
+  const double* mu_p2;
+  const double* cos_p1;
+  const double* cos_p2;
+  double* mu_out;
+  double* cos_out;
+  double* usum;
+  double* musum;
+  double* gIc;
+};
+
+__global__ void __launch_bounds__(256) k_adj_a(AdjArgs a, Tables t, double* __restrict__ u) {
+  const int64_t NjW = (int64_t)a.Nj * a.W;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = e / a.W, w = e - j * a.W;
+    double v = view_at(a.G, j, w);
+    const double ic = __ldg(t.Ic + (t.ic_per_w ? e : j));
+    if (a.mu_p1) v = fma(fma(2.0 * ic, a.cos_p1[e], __ldg(t.coef + j)), a.mu_p1[e], v);
+    if (a.mu_p2) v = fma(fma(-ic, a.cos_p2[e], __ldg(t.coef + a.Nj + j)), a.mu_p2[e], v);
+    const double uu = v * __ldg(t.inv_c0 + j);
+    u[e] = uu;
+    a.usum[e] += uu;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_adj_mu(AdjArgs a, Tables t, const double* __restrict__ u,
+                                                const double* __restrict__ nu) {
+  const int64_t NjW = (int64_t)a.Nj * a.W;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = e / a.W, w = e - j * a.W;
+    const int p0 = __ldg(t.jf_face + 2 * j), p1 = __ldg(t.jf_face + 2 * j + 1);
+    double y = p0 >= 0 ? signed_by(nu[(int64_t)(p0 >> 1) * a.W + w], p0 & 1) : 0.0;
+    if (p1 >= 0) y += signed_by(nu[(int64_t)(p1 >> 1) * a.W + w], p1 & 1);
+    const double mu = fma(y, __ldg(t.inv_c0 + j), -u[e]);
+    double s, c;
+    fast_sincos(fma(2.0, a.th_m1[e], -a.th_m2[e]), t.sincos, s, c);
+    a.mu_out[e] = mu;
+    a.cos_out[e] = c;
+    a.gIc[e] = fma(mu, s, a.gIc[e]);
+    a.musum[e] += mu;
+  }
+}
+
+__global__ void k_unpermute_scaled(const double* __restrict__ src, double* __restrict__ dst,
+                                   const int32_t* __restrict__ perm, int n, int W, double scale) {
+  const int64_t nW = (int64_t)n * W;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nW; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / W, w = e - i * W;
+    dst[(int64_t)__ldg(perm + i) * W + w] = scale * src[e];
+  }
+}
+
 __global__ void k_eval_sin(const double* __restrict__ x, double* __restrict__ out, int64_t n,
                            const double2* __restrict__ tab) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -770,18 +869,30 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
       // final multiply). "resistive": width 3 and c2 = Cv = 0 everywhere, in which case
       // c1 = -Rv - 2 Cv = -c0 exactly and c1/c0 = -1 (time_evolution.py:477-478, 489)
       const int nk = d->stencil_width - 1;
-      std::vector<double> icq(Nj), coefq((size_t)nk * Nj), rvq(Nj);
+      const size_t nic = d->Ic_w ? (size_t)Nj * d->W : (size_t)Nj;
+      std::vector<double> icq(nic), ic(nic), coefq((size_t)nk * Nj), rvq(Nj);
       bool resistive = d->stencil_width == 3;
       for (int j = 0; j < Nj; ++j) {
         const double ic0 = d->inv_c0[j];
-        icq[j] = d->Ic[j] * ic0;
+        if (d->Ic_w) {
+          for (int w = 0; w < d->W; ++w) {
+            ic[(size_t)j * d->W + w] = d->Ic_w[(size_t)j * d->W + w];
+            icq[(size_t)j * d->W + w] = d->Ic_w[(size_t)j * d->W + w] * ic0;
+          }
+        } else {
+          ic[j] = d->Ic[j];
+          icq[j] = d->Ic[j] * ic0;
+        }
         rvq[j] = d->Rv[j] * ic0 * ic0;
         for (int k = 0; k < nk; ++k) coefq[(size_t)k * Nj + j] = d->coef[(size_t)k * Nj + j] * ic0;
         if (resistive) resistive = d->coef[(size_t)Nj + j] == 0.0;
       }
       p->resistive = resistive ? 1 : 0;
+      p->t.ic_per_w = d->Ic_w ? 1 : 0;
+      p->t.Ic = p->up(ic.data(), ic.size());
       p->t.Icq = p->up(icq.data(), icq.size());
       p->t.coefq = p->up(coefq.data(), coefq.size());
+      p->t.coef = p->up(d->coef, (size_t)nk * Nj);
       p->t.Rvq = p->up(rvq.data(), rvq.size());
     }
     p->t.inv_c0 = p->up(d->inv_c0, Nj);
@@ -1013,6 +1124,51 @@ int jja_solve_static(jja_plan* p, const double* b, double* x, void* stream) {
     launch_levels_into(p, st, true, bx, z, nullptr);
     launch_levels_into(p, st, false, nullptr, z, bx);
     k_permute_rows<<<grid_for(NfW, 256), 256, 0, st>>>(bx, x, p->perm, p->Nf, p->W, 0);
+    g_launches++;
+    JJA_CUDA(cudaGetLastError());
+  });
+}
+
+int jja_adjoint_step(jja_plan* p, const jja_adjoint_args* g, void* stream) {
+  return guarded([&] {
+    if (!p || !g) throw Error(JJA_ERR_ARG, "jja_adjoint_step: null argument");
+    if (p->width != 3) throw Error(JJA_ERR_ARG, "jja_adjoint_step: the adjoint supports stencil width 3 only");
+    if (!g->th_m1 || !g->th_m2 || !g->mu_out || !g->cos_out || !g->usum || !g->musum || !g->gIc)
+      throw Error(JJA_ERR_ARG, "jja_adjoint_step: missing buffer");
+    if ((g->mu_p1 && !g->cos_p1) || (g->mu_p2 && !g->cos_p2))
+      throw Error(JJA_ERR_ARG, "jja_adjoint_step: mu of a later step given without its cos(phi)");
+    cudaStream_t st = (cudaStream_t)stream;
+    AdjArgs a{};
+    a.Nj = p->Nj; a.W = p->W; a.G = g->G;
+    a.th_m1 = g->th_m1; a.th_m2 = g->th_m2;
+    a.mu_p1 = g->mu_p1; a.mu_p2 = g->mu_p2; a.cos_p1 = g->cos_p1; a.cos_p2 = g->cos_p2;
+    a.mu_out = g->mu_out; a.cos_out = g->cos_out; a.usum = g->usum; a.musum = g->musum; a.gIc = g->gIc;
+    const int64_t NjW = (int64_t)p->Nj * p->W, NfW = (int64_t)p->Nf * p->W;
+    k_adj_a<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj);
+    StepArgs s{};
+    s.Nj = p->Nj; s.Nf = p->Nf; s.W = p->W; s.width = p->width; s.d_step = p->d_step;
+    k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(s, p->t, p->xj, p->b);
+    g_launches += 2;
+    launch_levels(p, st, true);
+    launch_levels(p, st, false);
+    k_adj_mu<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj, p->x);
+    g_launches++;
+    JJA_CUDA(cudaGetLastError());
+  });
+}
+
+int jja_adjoint_flux(jja_plan* p, const double* usum, double* gf, void* stream) {
+  return guarded([&] {
+    if (!p || !usum || !gf) throw Error(JJA_ERR_ARG, "jja_adjoint_flux: null argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t NfW = (int64_t)p->Nf * p->W;
+    StepArgs s{};
+    s.Nj = p->Nj; s.Nf = p->Nf; s.W = p->W; s.width = p->width; s.d_step = p->d_step;
+    k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(s, p->t, usum, p->b);
+    g_launches++;
+    launch_levels(p, st, true);
+    launch_levels(p, st, false);
+    k_unpermute_scaled<<<grid_for(NfW, 256), 256, 0, st>>>(p->x, gf, p->perm, p->Nf, p->W, -kTwoPi);
     g_launches++;
     JJA_CUDA(cudaGetLastError());
   });

@@ -113,7 +113,7 @@ class HostFactor:
 class DevicePlan:
     """Circuit tables + factor uploaded for W problems (owned C object)."""
 
-    def __init__(self, circuit, factor, A, W, dt, stencil_width, stencil):
+    def __init__(self, circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=None):
         Nj, Nf = circuit._Nj(), circuit._Nf()
         Rv, Cv, coef = coefficients(circuit, dt, stencil)
         Acsr = scipy.sparse.csr_matrix(A)
@@ -123,13 +123,15 @@ class DevicePlan:
             col=np.ascontiguousarray(Acsr.indices, np.int32),
             val=np.ascontiguousarray(Acsr.data, np.float64),
             Ic=np.ascontiguousarray(circuit._Ic(), np.float64),
+            Ic_w=None if Ic_w is None else np.ascontiguousarray(Ic_w, np.float64),
             inv_c0=np.ascontiguousarray(1.0 / coef[0], np.float64),
             coef=np.ascontiguousarray(np.stack(coef[1:]), np.float64),
             Rv=np.ascontiguousarray(Rv, np.float64))
         k = self._keep
         ex = (ctypes.c_double * 4)(*(list(EXTRAP[stencil_width]) + [0.0] * (4 - len(EXTRAP[stencil_width]))))
         d = N.PlanDesc(Nj, Nf, W, stencil_width, N.ptr(k["rowptr"], ctypes.c_int64), N.ptr(k["col"], ctypes.c_int32),
-                       N.ptr(k["val"]), N.ptr(k["Ic"]), N.ptr(k["inv_c0"]), N.ptr(k["coef"]), N.ptr(k["Rv"]), ex, dt)
+                       N.ptr(k["val"]), N.ptr(k["Ic"]), N.ptr(k["inv_c0"]), N.ptr(k["coef"]), N.ptr(k["Rv"]), ex, dt,
+                       N.ptr(k["Ic_w"]))
         h = ctypes.c_void_p()
         N.check(N.lib().jja_plan_create(ctypes.byref(d), factor.handle, ctypes.byref(h)))
         self.handle = h
@@ -189,14 +191,17 @@ def get_factor(circuit, dt, nd_leaf=8, ordering="nd", relax=(-1, -1.0)):
     return _FACTORS[key][0], A, key
 
 
-def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=8, ordering="nd", relax=(-1, -1.0)):
+def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=8, ordering="nd", relax=(-1, -1.0), Ic_w=None):
+    """Device plan for W problems; ``Ic_w`` (Nj, W) gives each problem its own critical currents."""
     factor, A, fkey = get_factor(circuit, dt, nd_leaf, ordering=ordering, relax=relax)
     Rv, Cv, coef = coefficients(circuit, dt, stencil)
-    key = (fkey, W, stencil_width, _digest(np.asarray(circuit._Ic(), np.float64), *coef, Rv,
-                                            A.indptr, A.indices, A.data))
+    if Ic_w is not None:
+        Ic_w = np.ascontiguousarray(np.broadcast_to(np.asarray(Ic_w, np.float64), (circuit._Nj(), W)))
+    ic = np.asarray(circuit._Ic(), np.float64) if Ic_w is None else Ic_w
+    key = (fkey, W, stencil_width, Ic_w is None, _digest(ic, *coef, Rv, A.indptr, A.indices, A.data))
     p = _PLANS.get(key)
     if p is None:
-        p = DevicePlan(circuit, factor, A, W, dt, stencil_width, stencil)
+        p = DevicePlan(circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=Ic_w)
         _PLANS[key] = p
         while len(_PLANS) > MAX_PLANS:
             _PLANS.popitem(last=False)
