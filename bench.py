@@ -124,6 +124,63 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def adjoint_leg(G, torch, Nt):
+    """Cost of gradients against a forward pass on the disorder workload: W = 64 copies of
+    SquareArray(64, 64), each with its own Ic ~ lognormal(0, 0.2) (seeded), f = 0.1, DC bias
+    1.2, T = 0, dt = 0.05, Nt steps; loss = mean voltage of the horizontal junctions over the
+    last Nt/2 steps; gradients w.r.t. every Ic, every face's f and the bias (sqrt(Nt) checkpoints).
+    Forward: the plain graph-replayed time stepping of the same problems (no checkpoints).
+    Gradient: checkpointed forward (loss) + backward (recompute + adjoint), wall clock."""
+    from pyjjasim_gb300.adjoint import AdjointRun, time_averaged_voltage_weights
+    from pyjjasim_gb300.backend import GpuSimulation
+    n, W = 64, 64
+    a = G.SquareArray(n, n)
+    Nj, Nf = a._Nj(), a._Nf()
+    Ic = np.random.default_rng(2024).lognormal(0.0, 0.2, (Nj, W))
+
+    def problem(steps):
+        Is = a.current_base(0.0)[:, None, None] * np.full(W, 1.2)[None, :, None]
+        return G.TimeEvolutionProblem(a, time_step=DT, time_step_count=steps, current_sources=Is, external_flux=0.1,
+                                      store_time_steps=[steps - 1], store_voltage=False, store_current=False)
+
+    horiz = np.arange(n * (n - 1))
+    t1, t2 = Nt - 1 - Nt // 2, Nt - 1
+    p = problem(Nt)
+    wts = time_averaged_voltage_weights(p, t1, t2, horiz)
+    warm = problem(64)
+    AdjointRun(warm, time_averaged_voltage_weights(warm, 30, 63, horiz), Ic=Ic).backward()   # plan + graphs
+    sim = GpuSimulation(p, Ic=Ic)
+    sim.run(64, use_graph=True)
+    sim.synchronize()
+    sim = GpuSimulation(p, Ic=Ic)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0.record(sim.stream)
+    sim.run(Nt, use_graph=True)
+    e1.record(sim.stream)
+    e1.synchronize()
+    t_fwd = time.perf_counter() - t0
+    fwd_dev = e0.elapsed_time(e1) / 1e3
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run = AdjointRun(p, wts, Ic=Ic)
+    t_ck = time.perf_counter() - t0
+    g = run.backward()
+    t_grad = time.perf_counter() - t0
+    ok = all(bool(torch.isfinite(v).all()) for v in g.values())
+    return {"workload": f"adjoint: W={W} x SquareArray({n},{n}), Ic~lognormal(0,0.2) per junction and problem "
+                        f"(seed 2024), f=0.1, DC bias 1.2, T=0, dt=0.05, {Nt} steps, loss = mean horizontal "
+                        f"junction voltage over steps {t1}..{t2}",
+            "Nj": Nj, "Nf": Nf, "W": W, "steps": Nt, "segments": len(run.segments),
+            "forward_seconds": t_fwd, "forward_device_seconds": fwd_dev,
+            "checkpointed_forward_seconds": t_ck, "backward_seconds": t_grad - t_ck,
+            "gradient_seconds": t_grad, "gradient_over_forward": t_grad / t_fwd,
+            "backward_over_forward": (t_grad - t_ck) / t_fwd,
+            "forward_junction_steps_per_s": Nj * W * Nt / t_fwd, "finite": ok,
+            "mean_loss": float(run.loss.mean().item())}
+
+
 def fp64_peak_tflops(torch):
     """Measured FP64 peak of this GPU: cuBLAS DGEMM 4096^3, best of 5."""
     n = 4096
@@ -246,6 +303,8 @@ def main():
     ap.add_argument("--W", type=int, default=W_BATCH, help="problems per launch (profiling mode)")
     ap.add_argument("--ordering", default="nd", choices=["nd", "mmd"], help="fill-reducing order of the factor")
     ap.add_argument("--relax", default="-1,-1", help="supernode amalgamation: max zeros,max fraction (-1: default)")
+    ap.add_argument("--adjoint-steps", type=int, default=5000,
+                    help="time steps of the adjoint-cost leg (0 skips it)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -386,6 +445,8 @@ def main():
                            "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
                            "time_steps_per_call": args.steps, "seconds_per_call": t_e2e,
                            "api": "pyjjasim_gb300.TimeEvolutionProblem(...).compute()"}
+        if args.adjoint_steps > 0:
+            line["adjoint"] = adjoint_leg(G, torch, args.adjoint_steps)
         if not args.no_cpu_baseline:
             rate, per_step = cpu_oracle_rate(W_BATCH, 6)
             line["cpu_baseline"] = {"value": rate, "unit": "junction-steps/s", "cores": os.cpu_count(),

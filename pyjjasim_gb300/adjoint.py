@@ -53,8 +53,8 @@ class AdjointRun:
         self.segments = [(s0, min(Nt, s0 + S)) for s0 in range(0, Nt, S)]
         self.Nt = Nt
         dev = sim.dev
-        self.G = {int(n): torch.from_numpy(np.ascontiguousarray(np.broadcast_to(g, (self.Nj, self.W)),
-                                                                np.float64)).to(dev)
+        self.G = {int(n): torch.from_numpy(np.array(np.broadcast_to(g, (self.Nj, self.W)), np.float64,
+                                                    order="C")).to(dev)
                   for n, g in loss_weights.items()}
         for n in self.G:
             if not 0 <= n < Nt:
