@@ -10,7 +10,12 @@ Reported (one JSON line):
   value       junction-steps/s with the state resident on the device (CUDA events around
               --steps graph-replayed steps on the launching stream);
   e2e         the same metric through the public API, TimeEvolutionProblem(...).compute(),
-              host inputs in, host results out (copies inside the timed region);
+              host inputs in, host results out (copies inside the timed region), on the
+              workload's full 10000 steps with steps 4999 and 9999 stored;
+  parity      the error against the FP64 CPU oracle: time-averaged voltages (tolerance 1e-6),
+              trajectories and vortex configurations of four problems after 1000 steps;
+  adjoint     cost of gradients (checkpointed adjoint) against a forward pass on the disorder
+              workload (64 x 64 arrays, W = 64, 5000 steps);
   plain_gpu   the same lattice, one problem per launch (W = 1);
   roofline    the dominant stage (forward supernodal solve) against the FP64 pipe, with
               its HBM figures beside it; stage times from CUDA events per stage;
@@ -150,9 +155,8 @@ def adjoint_leg(G, torch, Nt):
     warm = problem(64)
     AdjointRun(warm, time_averaged_voltage_weights(warm, 30, 63, horiz), Ic=Ic).backward()   # plan + graphs
     sim = GpuSimulation(p, Ic=Ic)
-    sim.run(64, use_graph=True)
+    sim.run(64, use_graph=True)     # captures this simulation's graph before the timed region
     sim.synchronize()
-    sim = GpuSimulation(p, Ic=Ic)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -179,6 +183,45 @@ def adjoint_leg(G, torch, Nt):
             "backward_over_forward": (t_grad - t_ck) / t_fwd,
             "forward_junction_steps_per_s": Nj * W * Nt / t_fwd, "finite": ok,
             "mean_loss": float(run.loss.mean().item())}
+
+
+PARITY_PROBLEMS = (150, 250, 350, 450)   # bias 0.59, 0.98, 1.37, 1.76: across the IV curve
+
+
+def parity_leg(G, Nt):
+    """Error of the batched GPU run against the FP64 CPU oracle on the headline workload:
+    all 512 problems on the GPU for Nt steps, four of them (PARITY_PROBLEMS) in the oracle;
+    time-averaged voltage of the horizontal junctions over the second half (the IV-curve
+    point), trajectories, and vortex configurations at the last step."""
+    from oracle import rcsj_oracle
+    t1, t2 = Nt // 2 - 1, Nt - 1
+    bias = bias_slice(0, 1)
+    a = G.SquareArray(NX, NY)
+    Is = a.current_base(0.0)[:, None, None] * bias[None, :, None]
+    p = G.TimeEvolutionProblem(a, time_step=DT, time_step_count=Nt, current_sources=Is, external_flux=FRUST,
+                               store_time_steps=[t1, t2], store_voltage=False, store_current=False)
+    th_g = p.compute().get_theta()[:, list(PARITY_PROBLEMS), :]
+    sel = np.asarray(bias)[list(PARITY_PROBLEMS)]
+    po = G.TimeEvolutionProblem(a, time_step=DT, time_step_count=Nt,
+                                current_sources=a.current_base(0.0)[:, None, None] * sel[None, :, None],
+                                external_flux=FRUST, store_time_steps=[t1, t2], store_voltage=False,
+                                store_current=False)
+    t0 = time.perf_counter()
+    th_o, _, _ = rcsj_oracle.time_evolution(po)
+    t_oracle = time.perf_counter() - t0
+    horiz = np.arange(NX * (NY - 1))     # current_base(0) drives the horizontal junctions
+    vbar = lambda th: (th[horiz, :, 1] - th[horiz, :, 0]).mean(0) / (DT * (t2 - t1))
+    v_g, v_o = vbar(th_g), vbar(th_o)
+    A = a.get_cycle_matrix()
+    vort = lambda th: -(A @ np.round(th[:, :, -1] / (2 * np.pi)))
+    return {"problems": list(PARITY_PROBLEMS), "bias": sel.tolist(), "steps": Nt,
+            "vbar_window": [t1, t2], "vbar_gpu": v_g.tolist(), "vbar_oracle": v_o.tolist(),
+            "max_abs_vbar_error": float(np.abs(v_g - v_o).max()), "tolerance": 1e-6,
+            "within_tolerance": bool(np.abs(v_g - v_o).max() <= 1e-6),
+            "max_abs_theta_error": float(np.abs(th_g - th_o).max()),
+            "vortex_configurations_equal": bool(np.array_equal(vort(th_g), vort(th_o))),
+            "oracle_seconds": t_oracle,
+            "oracle": "numpy/scipy restatement of the reference loop (pinned to the reference's golden outputs)"}
 
 
 def fp64_peak_tflops(torch):
@@ -270,8 +313,9 @@ def run_reference(args):
 def profile_mode(args):
     """Minimal launch sequence for ncu: every kernel launch of a step is issued eagerly.
 
-    Launch order per step: k_junction, k_face_rhs, k_fwd_level x n_levels (leaves first),
-    k_bwd_level x n_levels (root first), k_update."""
+    Launch order: per run k_scale_sources, k_junction (q of its first step); per step
+    k_face_rhs, k_zero_rows, k_fwd_level x n_levels (leaves first), k_zero_rows,
+    k_bwd_level x n_levels (root first), k_update (theta_next and the next step's q)."""
     import torch
     import pyjjasim_gb300 as G
     from pyjjasim_gb300.backend import GpuSimulation
@@ -305,6 +349,10 @@ def main():
     ap.add_argument("--relax", default="-1,-1", help="supernode amalgamation: max zeros,max fraction (-1: default)")
     ap.add_argument("--adjoint-steps", type=int, default=5000,
                     help="time steps of the adjoint-cost leg (0 skips it)")
+    ap.add_argument("--e2e-steps", type=int, default=10000,
+                    help="time steps of the end-to-end compute() call (the workload's 10000)")
+    ap.add_argument("--parity-steps", type=int, default=1000,
+                    help="time steps of the oracle comparison on four of the problems (0 skips it)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -369,11 +417,14 @@ def main():
     value = Nj * W * args.steps * world / el
     clocks = clk.summary()
     # graph replays are counted at capture time only: count the kernels of one eager step
+    # (a 2-step run minus a 1-step run) and the few every run starts with
     n1 = lib.jja_launch_count()
     sim.run(1, use_graph=False)
+    n2 = lib.jja_launch_count()
+    sim.run(2, use_graph=False)
     sim.synchronize()
-    per_step_launches = lib.jja_launch_count() - n1
-    gpu_launches = per_step_launches * args.steps
+    per_step_launches = (lib.jja_launch_count() - n2) - (n2 - n1)
+    gpu_launches = per_step_launches * args.steps + (n2 - n1 - per_step_launches)
 
     # per-stage device time (eager, CUDA events at the stage boundaries of every step)
     stages = sim.run_timed(args.steps)
@@ -430,21 +481,34 @@ def main():
         del sim1
         # end to end through the public API with host buffers
         if not args.no_e2e:
-            pe = make_problem(G, args.steps, bias)
-            pe.compute(**factor_opts(args))               # warm: plan cache, graph capture
+            # the workload as a user runs it: Nt steps, steps Nt/2-1 and Nt-1 stored, the IV-curve
+            # point read from them on the host (config: 10000 steps, the first 5000 discarded)
+            Ne = args.e2e_steps
+            make_problem(G, 64, bias).compute(**factor_opts(args))     # warm: plan cache, modules
             torch.cuda.synchronize()
             t0 = time.perf_counter()
+            a = G.SquareArray(NX, NY)
+            pe = G.TimeEvolutionProblem(a, time_step=DT, time_step_count=Ne,
+                                        current_sources=a.current_base(0.0)[:, None, None] * bias[None, :, None],
+                                        external_flux=FRUST, store_time_steps=[Ne // 2 - 1, Ne - 1])
             res = pe.compute(**factor_opts(args))
-            th = res.get_theta()
+            V = res.get_voltage()
+            vbar = (res.get_theta()[:NX * (NY - 1), :, 1] - res.get_theta()[:NX * (NY - 1), :, 0]).mean(0) \
+                / (DT * (Ne - Ne // 2))
             t_e2e = time.perf_counter() - t0
-            assert np.isfinite(th).all()
+            assert np.isfinite(V).all() and np.isfinite(vbar).all()
             stored = (pe.store_time_steps | np.roll(pe.store_time_steps, -1))  # V needs the previous step
             h2d = (2 * Nj * W + Nj * W) * 8 + 8           # theta(t-1), theta(t-2), Is (Nj x W), f (scalar)
             d2h = (int(stored.sum()) + int(pe.store_time_steps.sum())) * Nj * W * 8
-            line["e2e"] = {"value": Nj * W * args.steps / t_e2e, "unit": "junction-steps/s",
-                           "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-                           "time_steps_per_call": args.steps, "seconds_per_call": t_e2e,
-                           "api": "pyjjasim_gb300.TimeEvolutionProblem(...).compute()"}
+            line["e2e"] = {"value": Nj * W * Ne / t_e2e, "unit": "junction-steps/s",
+                           "h2d_bytes_per_step": h2d / Ne, "d2h_bytes_per_step": d2h / Ne,
+                           "time_steps_per_call": Ne, "seconds_per_call": t_e2e,
+                           "stored_steps": [Ne // 2 - 1, Ne - 1],
+                           "iv_curve_vbar_min_max": [float(vbar.min()), float(vbar.max())],
+                           "api": "pyjjasim_gb300.TimeEvolutionProblem(...).compute(), inputs built on the "
+                                  "host inside the timed region, results (theta, I, V) back on the host"}
+        if args.parity_steps > 0:
+            line["parity"] = parity_leg(G, args.parity_steps)
         if args.adjoint_steps > 0:
             line["adjoint"] = adjoint_leg(G, torch, args.adjoint_steps)
         if not args.no_cpu_baseline:

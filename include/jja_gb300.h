@@ -104,12 +104,16 @@ void jja_plan_destroy(jja_plan* p);
 /* Bytes of device memory held by the plan (tables + factor + work vectors). */
 int64_t jja_plan_device_bytes(const jja_plan* p);
 
-/* A per-step source on the device: value(n, w) = ptr[n*stride_n + w*stride_w]
- * (element strides; 0 broadcasts). ptr == NULL means the source is identically zero. */
+/* A source on the device: at step i, value(n, w) = ptr[n*stride_n + w*stride_w + (i - t0)*stride_t]
+ * (element strides; 0 broadcasts). stride_t == 0: the same value at every step. stride_t != 0:
+ * a window of time steps [t0, t0 + steps) held on the device (t0 and steps are jja_state.src_t0
+ * and src_steps), which replaces the reference's per-step evaluation of time-dependent inputs
+ * (time_evolution.py:334-340, 523-531). ptr == NULL means the source is identically zero. */
 typedef struct {
   const double* ptr;
   int64_t stride_n;
   int64_t stride_w;
+  int64_t stride_t;
 } jja_view;
 
 enum { JJA_NOISE_NONE = 0, JJA_NOISE_BUFFER = 1, JJA_NOISE_PHILOX = 2 };
@@ -128,12 +132,16 @@ typedef struct {
   int64_t step;          /* index of the first step of the call (Philox counter) */
   double* th_out;        /* device (slots x Nj x W) or NULL */
   double* I_out;         /* device (slots x Nj x W) or NULL */
+  int64_t src_t0;        /* first step held by the time-dependent views (stride_t != 0) */
+  int64_t src_steps;     /* steps they hold: a call must satisfy src_t0 <= step and
+                            step + nsteps <= src_t0 + src_steps */
 } jja_state;
 
 /* Runs nsteps time steps of the RCSJ update (time_evolution.py:523-580) on `stream`
  * (a cudaStream_t, NULL = default stream). th_slot[i] / I_slot[i] (host arrays of length
- * nsteps, or NULL) give the output slot of step i or -1. With use_graph != 0 the step
- * sequence is captured once into a CUDA graph and replayed. */
+ * nsteps, or NULL) give the output slot of step i or -1. With use_graph != 0 runs of steps
+ * that store nothing are captured into CUDA graphs (a few are cached per plan, keyed by the
+ * state's buffers) and replayed. */
 int jja_run(jja_plan* p, jja_state* st, int nsteps, const int64_t* th_slot, const int64_t* I_slot,
             int use_graph, void* stream);
 

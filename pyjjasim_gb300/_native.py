@@ -36,13 +36,13 @@ class PlanDesc(ctypes.Structure):
 
 
 class View(ctypes.Structure):
-    _fields_ = [("ptr", c_void_p), ("stride_n", c_int64), ("stride_w", c_int64)]
+    _fields_ = [("ptr", c_void_p), ("stride_n", c_int64), ("stride_w", c_int64), ("stride_t", c_int64)]
 
 
 class State(ctypes.Structure):
     _fields_ = [("hist", c_void_p * 4), ("theta_s", c_void_p), ("Is", View), ("f", View), ("Vs", View), ("T", View),
                 ("noise_mode", c_int), ("noise", c_void_p), ("seed", ctypes.c_uint64), ("step", c_int64),
-                ("th_out", c_void_p), ("I_out", c_void_p)]
+                ("th_out", c_void_p), ("I_out", c_void_p), ("src_t0", c_int64), ("src_steps", c_int64)]
 
 
 class AdjointArgs(ctypes.Structure):

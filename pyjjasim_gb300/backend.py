@@ -53,39 +53,84 @@ def _source_is_zero(timedep, getter, N_rows, W):
     return bool(np.all(np.abs(v) <= 1e-8))
 
 
-class _Source:
-    """A source (Is, f, Vs or T) on the device as a strided view, updated per step if time-dependent."""
+_WINDOW_BYTES = 256 << 20   # device bytes of one window of a time-dependent source
+_WINDOW_MAX_STEPS = 4096
 
-    def __init__(self, torch, dev, stream, getter, timedep, N_rows, W, zero):
-        self.getter, self.timedep, self.N, self.W = getter, timedep, N_rows, W
+
+class _Source:
+    """A source (Is, f, Vs or T) on the device as a strided ``jja_view``.
+
+    Time-independent: one (rows, cols) array, broadcast axes stored once.
+    Time-dependent (an (N, W, Nt) array or a callable of the step, time_evolution.py:334-340):
+    windows of K consecutive steps stored time-major (K, rows, cols) that the kernels index
+    by the on-device step counter. The host fills a window in pinned memory and uploads it
+    asynchronously on the simulation's stream; two window slots alternate, so the host
+    evaluates window k+1 while the GPU steps through window k.
+    """
+
+    def __init__(self, torch, dev, stream, getter, raw, timedep, N_rows, W, Nt, zero):
+        self.getter, self.raw, self.timedep, self.N, self.W, self.Nt = getter, raw, timedep, N_rows, W, Nt
+        self.torch, self.dev, self.stream = torch, dev, stream
         self.zero = zero
-        self.buf = None
-        self.view = N.View(None, 0, 0)
+        self.view = N.View(None, 0, 0, 0)
         self.h2d_bytes = 0
         if zero:
             return
-        v0 = np.broadcast_to(np.asarray(getter(0), dtype=np.float64), (N_rows, W))
-        if timedep:
-            rows, cols = N_rows, W        # a later step may not broadcast like step 0: keep it full
-        else:
+        if not timedep:
+            v0 = np.broadcast_to(np.asarray(getter(0), dtype=np.float64), (N_rows, W))
             rows, cols = _compact(v0).shape
-        self.shape = (rows, cols)
-        self.buf = torch.empty(self.shape, dtype=torch.float64, device=dev)
-        self.view = N.View(self.buf.data_ptr(), cols if rows > 1 else 0, 1 if cols > 1 else 0)
-        self.torch, self.stream = torch, stream
-        self.load(0, v0)
-
-    def load(self, i, value=None):
-        if self.zero:
+            self.shape = (rows, cols)
+            self.buf = torch.empty(self.shape, dtype=torch.float64, device=dev)
+            self.view = N.View(self.buf.data_ptr(), cols if rows > 1 else 0, 1 if cols > 1 else 0, 0)
+            host = np.array(v0[:rows, :cols], dtype=np.float64, order="C")
+            with torch.cuda.stream(stream):
+                self.buf.copy_(torch.from_numpy(host))
+            self.h2d_bytes += host.nbytes
             return
-        v = np.broadcast_to(np.asarray(self.getter(i) if value is None else value, np.float64), (self.N, self.W))
-        r, c = self.shape
-        host = np.ascontiguousarray(v[:r, :c])
-        if not host.flags.writeable:      # a broadcast view: torch.from_numpy wants writable memory
-            host = host.copy()
-        with self.torch.cuda.stream(self.stream):
-            self.buf.copy_(self.torch.from_numpy(host))
-        self.h2d_bytes += host.nbytes
+        if callable(raw) or not isinstance(raw, np.ndarray) or raw.ndim != 3:
+            rows, cols = N_rows, W        # a callable may change its shape between steps: keep it full
+        else:
+            rows, cols = _compact(raw[:, :, 0]).shape
+        self.shape = (rows, cols)
+        self.K = int(max(1, min(_WINDOW_MAX_STEPS, Nt, _WINDOW_BYTES // (8 * rows * cols))))
+        self.slots = [None, None]         # per slot: [window index, device buffer, pinned buffer, event]
+
+    def _fill(self, host, t0, n):
+        """Steps [t0, t0 + n) into host[:n] (time-major)."""
+        rows, cols = self.shape
+        if callable(self.raw) or not isinstance(self.raw, np.ndarray) or self.raw.ndim != 3:
+            for k in range(n):
+                host[k] = np.broadcast_to(np.asarray(self.getter(t0 + k), np.float64), (self.N, self.W))[:rows, :cols]
+        else:
+            host[:n] = np.moveaxis(self.raw[:rows, :cols, t0:t0 + n], 2, 0)
+
+    def upload_window(self, wi, K):
+        """Fill window wi (steps [wi K, wi K + K) within Nt) and enqueue its upload into slot wi % 2."""
+        torch = self.torch
+        s = wi % 2
+        rows, cols = self.shape
+        if self.slots[s] is None:
+            self.slots[s] = [-1, torch.empty((K, rows, cols), dtype=torch.float64, device=self.dev),
+                             torch.empty((K, rows, cols), dtype=torch.float64, pin_memory=True), None]
+        slot = self.slots[s]
+        if slot[0] == wi:
+            return
+        if slot[3] is not None:
+            slot[3].synchronize()         # the previous upload from this pinned buffer is done
+        t0 = wi * K
+        n = min(K, self.Nt - t0)
+        self._fill(slot[2].numpy(), t0, n)
+        with torch.cuda.stream(self.stream):
+            slot[1][:n].copy_(slot[2][:n], non_blocking=True)
+            slot[3] = torch.cuda.Event()
+            slot[3].record(self.stream)
+        slot[0] = wi
+        self.h2d_bytes += n * rows * cols * 8
+
+    def use_window(self, wi):
+        rows, cols = self.shape
+        buf = self.slots[wi % 2][1]
+        self.view = N.View(buf.data_ptr(), cols if rows > 1 else 0, 1 if cols > 1 else 0, rows * cols)
 
 
 class _NumpyNoise:
@@ -140,7 +185,7 @@ class GpuSimulation:
             self.hist = []
             with torch.cuda.stream(self.stream):
                 for h in hist0:
-                    h = np.ascontiguousarray(np.broadcast_to(h, (self.Nj, self.W)), np.float64)
+                    h = np.array(np.broadcast_to(h, (self.Nj, self.W)), np.float64, order="C")
                     zero = not np.any(h)
                     self.hist0_zero.append(zero)
                     if zero:      # the default initial condition: no host->device copy needed
@@ -149,12 +194,19 @@ class GpuSimulation:
                         self.hist.append(torch.from_numpy(h).to(self.dev))
                         self.h2d_bytes += h.nbytes
             self.srcs = {}
-            for name, getter, td, rows in (("Is", problem._Is, problem._Is_is_timedep, self.Nj),
-                                           ("f", problem._f, problem._f_is_timedep, self.Nf),
-                                           ("Vs", problem._Vs, problem._Vs_is_timedep, self.Nj),
-                                           ("T", problem._T, problem._T_is_timedep, self.Nj)):
+            self.Nt = problem._Nt()
+            for name, getter, td, rows, attr in (
+                    ("Is", problem._Is, problem._Is_is_timedep, self.Nj, "current_sources"),
+                    ("f", problem._f, problem._f_is_timedep, self.Nf, "external_flux"),
+                    ("Vs", problem._Vs, problem._Vs_is_timedep, self.Nj, "voltage_sources"),
+                    ("T", problem._T, problem._T_is_timedep, self.Nj, "temperature")):
                 zero = _source_is_zero(td, getter, rows, self.W)
-                self.srcs[name] = _Source(torch, self.dev, self.stream, getter, td, rows, self.W, zero)
+                self.srcs[name] = _Source(torch, self.dev, self.stream, getter, getattr(problem, attr, None), td,
+                                          rows, self.W, self.Nt, zero)
+            # time-dependent sources share one grid of step windows
+            self.windowed = [s for s in self.srcs.values() if s.timedep and not s.zero]
+            self.window_K = min((s.K for s in self.windowed), default=0)
+            self.window = -1
             self.h2d_bytes += sum(s.h2d_bytes for s in self.srcs.values())
             Vs_zero, T_zero = self.srcs["Vs"].zero, self.srcs["T"].zero
             self.theta_s = None if Vs_zero else torch.zeros((self.Nj, self.W), dtype=torch.float64, device=self.dev)
@@ -181,9 +233,36 @@ class GpuSimulation:
                 st.noise_mode = N.NOISE_BUFFER
                 self.noise_buf = torch.empty((self.Nj, self.W), dtype=torch.float64, device=self.dev)
                 st.noise = self.noise_buf.data_ptr()
-            self.per_step_host = self.noise_gen is not None or any(s.timedep and not s.zero for s in self.srcs.values())
+            self.per_step_host = self.noise_gen is not None
 
     # ----------------------------------------------------------------------------------------
+    def _enter_window(self, step):
+        """Make the window holding ``step`` current (uploading it if it is not already there);
+        returns the number of steps from ``step`` to the end of the window."""
+        if not self.windowed:
+            return None
+        if step >= self.Nt:
+            raise ValueError(f"step {step} is past the time-dependent sources ({self.Nt} steps)")
+        K = self.window_K
+        wi = step // K
+        if wi != self.window:
+            for s in self.windowed:
+                s.upload_window(wi, K)
+                s.use_window(wi)
+            st = self.state
+            st.Is, st.f, st.Vs, st.T = (self.srcs[k].view for k in ("Is", "f", "Vs", "T"))
+            st.src_t0 = wi * K
+            st.src_steps = min(K, self.Nt - wi * K)
+            self.window = wi
+        return self.state.src_t0 + self.state.src_steps - step
+
+    def _prefetch_window(self):
+        """Fill and enqueue the window after the current one (host work that overlaps the GPU)."""
+        nxt = self.window + 1
+        if self.windowed and nxt * self.window_K < self.Nt:
+            for s in self.windowed:
+                s.upload_window(nxt, self.window_K)
+
     def run(self, nsteps, th_slot=None, I_slot=None, th_dev=None, I_dev=None, use_graph=True):
         """Advance nsteps steps; step i writes th_dev[th_slot[i]] / I_dev[I_slot[i]] when >= 0."""
         torch, st = self.torch, self.state
@@ -193,26 +272,33 @@ class GpuSimulation:
         th_slot = None if th_slot is None else np.ascontiguousarray(th_slot, np.int64)
         I_slot = None if I_slot is None else np.ascontiguousarray(I_slot, np.int64)
         h = ctypes.c_void_p(self.stream.cuda_stream)
-        if not self.per_step_host:
-            N.check(lib.jja_run(self.plan.handle, ctypes.byref(st), int(nsteps), N.ptr(th_slot, ctypes.c_int64),
-                                N.ptr(I_slot, ctypes.c_int64), int(use_graph), h))
-            return
-        for k in range(nsteps):
-            i = st.step
-            for s in self.srcs.values():
-                if s.timedep and not s.zero and i > 0:
-                    s.load(i)
-            if self.noise_gen is not None:
-                with torch.cuda.stream(self.stream):
-                    self.noise_buf.copy_(torch.from_numpy(np.ascontiguousarray(self.noise_gen(i), np.float64)))
-            N.check(lib.jja_run(self.plan.handle, ctypes.byref(st), 1,
-                                N.ptr(th_slot[k:k + 1], ctypes.c_int64) if th_slot is not None else None,
-                                N.ptr(I_slot[k:k + 1], ctypes.c_int64) if I_slot is not None else None, 0, h))
+        k = 0
+        while k < nsteps:
+            left = self._enter_window(st.step)
+            n = nsteps - k if left is None else min(nsteps - k, left)
+            ts = None if th_slot is None else th_slot[k:k + n]
+            Is_ = None if I_slot is None else I_slot[k:k + n]
+            if not self.per_step_host:
+                N.check(lib.jja_run(self.plan.handle, ctypes.byref(st), int(n), N.ptr(ts, ctypes.c_int64),
+                                    N.ptr(Is_, ctypes.c_int64), int(use_graph), h))
+                self._prefetch_window()
+            else:
+                for q in range(n):
+                    with torch.cuda.stream(self.stream):
+                        self.noise_buf.copy_(torch.from_numpy(
+                            np.array(self.noise_gen(st.step), np.float64, order="C")))
+                    N.check(lib.jja_run(self.plan.handle, ctypes.byref(st), 1,
+                                        N.ptr(ts[q:q + 1], ctypes.c_int64) if ts is not None else None,
+                                        N.ptr(Is_[q:q + 1], ctypes.c_int64) if Is_ is not None else None, 0, h))
+            k += n
 
     def run_timed(self, nsteps):
         """Advance nsteps steps (eager) and return per-stage device milliseconds."""
         if self.per_step_host:
-            raise ValueError("run_timed needs device-resident sources and on-device noise")
+            raise ValueError("run_timed needs on-device noise")
+        left = self._enter_window(self.state.step)
+        if left is not None and left < nsteps:
+            raise ValueError("run_timed: the steps cross a window of the time-dependent sources")
         ms = np.zeros(6)
         N.check(N.lib().jja_run_timed(self.plan.handle, ctypes.byref(self.state), int(nsteps), N.ptr(ms),
                                       ctypes.c_void_p(self.stream.cuda_stream)))

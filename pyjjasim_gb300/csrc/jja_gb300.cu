@@ -88,8 +88,9 @@ __device__ __forceinline__ double philox_normal(uint64_t seed, uint64_t elem, ui
   return (double)(rad * cospif(2.0f * u2));
 }
 
-__device__ __forceinline__ double view_at(const jja_view& v, int64_t n, int64_t w) {
-  return v.ptr ? __ldg(v.ptr + n * v.stride_n + w * v.stride_w) : 0.0;
+// value of a source at (n, w) in time slot tt = step - window start (ignored when stride_t == 0)
+__device__ __forceinline__ double view_at(const jja_view& v, int64_t n, int64_t w, int64_t tt = 0) {
+  return v.ptr ? __ldg(v.ptr + n * v.stride_n + w * v.stride_w + tt * v.stride_t) : 0.0;
 }
 
 struct StepArgs {
@@ -101,13 +102,16 @@ struct StepArgs {
   int noise_mode;
   const double* noise;
   uint64_t seed;
+  // device counters: [0] step whose face RHS comes next (written by k_update), [1] that step + 1
+  // (written by k_face_rhs), [2] first step of the time-dependent source window. Each kernel
+  // writes only a slot that no other thread of the same launch reads.
   int64_t* d_step;
   int64_t th_slot, I_slot;
   double* th_out;
   double* I_out;
   double e[4];
   double dt;
-  jja_view Isq;        // Is / c0 (plan-owned buffer refreshed at the start of a run)
+  jja_view Isq;        // Is / c0 for a time-independent Is (plan-owned, refreshed at the start of a run)
   int resistive;       // width 3 and no capacitance anywhere: c1 / c0 = -1, c2 = 0
 };
 
@@ -221,8 +225,9 @@ __device__ __forceinline__ void fast_sincos(double x, const double2* __restrict_
 // evaluated with the coefficients already divided by c0 (Icq = Ic/c0, coefq_k = c_k/c0,
 // Rvq = Rv/c0^2, Isq = Is/c0), which saves the final multiply. Without capacitance
 // (stencil width 3) c1/c0 = -1 and c2 = 0 exactly, so x/c0 = Icq sin - th1 - Isq.
+// `step` keys the Philox stream; tt = step - window start indexes time-dependent sources.
 __device__ __forceinline__ double junction_q(const StepArgs& a, const Tables& t, int64_t e, int64_t j, int64_t w,
-                                            const double* th, int64_t step) {
+                                            const double* th, int64_t step, int64_t tt) {
   double arg;
   if (a.width == 3) {
     arg = fma(2.0, th[0], -th[1]);        // 2 th1 - th2 with the reference's single rounding
@@ -243,12 +248,14 @@ __device__ __forceinline__ double junction_q(const StepArgs& a, const Tables& t,
     for (int k = 0; k < 4; ++k)
       if (k < a.width - 1) X = fma(__ldg(t.coefq + (int64_t)k * a.Nj + j), th[k], X);
   }
+  // Is / c0: precomputed when Is does not change with time, else scaled here
+  const double isq = a.Isq.ptr ? view_at(a.Isq, j, w) : view_at(a.Is, j, w, tt) * __ldg(t.inv_c0 + j);
   if (a.noise_mode == JJA_NOISE_NONE)
-    return a.Isq.ptr ? X - view_at(a.Isq, j, w) : X;   // (0 - Is) + X in the reference
-  const double T = view_at(a.T, j, w);
+    return a.Is.ptr ? X - isq : X;   // (0 - Is) + X in the reference
+  const double T = view_at(a.T, j, w, tt);
   const double xi = a.noise_mode == JJA_NOISE_BUFFER ? a.noise[e] : philox_normal(a.seed, (uint64_t)e, (uint64_t)step);
   const double fl = sqrt(2.0 * T * __ldg(t.Rvq + j)) * xi;
-  return (fl - view_at(a.Isq, j, w)) + X;
+  return (fl - isq) + X;
 }
 
 // Isq = Is / c0 per junction, refreshed at the start of every run (and every host-driven step)
@@ -264,21 +271,30 @@ __global__ void __launch_bounds__(256) k_scale_sources(jja_view Is, const double
 // q for the first step of a run, from the stored phase history
 __global__ void __launch_bounds__(256) k_junction(StepArgs a, Tables t, double* __restrict__ q) {
   const int64_t NjW = (int64_t)a.Nj * a.W;
-  const int64_t step = *a.d_step;
+  const int64_t step = a.d_step[0], tt = step - a.d_step[2];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = e / a.W, w = e - j * a.W;
     double th[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) th[k] = (k < a.width - 1) ? a.h[k][e] : 0.0;
-    q[e] = junction_q(a, t, e, j, w, th, step);
+    q[e] = junction_q(a, t, e, j, w, th, step, tt);
   }
 }
 
+// the step counters at the start of a call (kernel arguments are fixed at launch, so the
+// host's values need no pinned staging)
+__global__ void k_set_counters(int64_t* __restrict__ d_step, int64_t step, int64_t t0) {
+  d_step[0] = step;
+  d_step[1] = step;
+  d_step[2] = t0;
+}
+
 // b(p, w) = sum_j A_pj (q_j - theta_s_j) - 2 pi f_p, p in the factor's face order. Also
-// advances the device step counter (read by the junction evaluations of the next step).
+// publishes step + 1 in d_step[1] (read by k_update, which evaluates the next step's q).
 __global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const double* __restrict__ q,
                                                   double* __restrict__ b) {
   const int64_t NfW = (int64_t)a.Nf * a.W;
+  const int64_t step = a.d_step[0], tt = step - a.d_step[2];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NfW; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = e / a.W, w = e - p * a.W;
     double acc = 0.0;
@@ -309,10 +325,10 @@ __global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const do
         acc = (i == i0) ? v : acc + v;
       }
     }
-    if (a.f.ptr) acc = fma(-kTwoPi, view_at(a.f, __ldg(t.face_orig + p), w), acc);
+    if (a.f.ptr) acc = fma(-kTwoPi, view_at(a.f, __ldg(t.face_orig + p), w, tt), acc);
     b[e] = acc;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) *a.d_step += 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.d_step[1] = step + 1;
 }
 
 // theta_next = (A^T J)/c0 - q, outputs, theta_s update (time_evolution.py:562-580); with
@@ -322,7 +338,8 @@ template <bool kFuseNext>
 __global__ void __launch_bounds__(256) k_update(StepArgs a, Tables t, double* __restrict__ q,
                                                 const double* __restrict__ J) {
   const int64_t NjW = (int64_t)a.Nj * a.W;
-  const int64_t next_step = *a.d_step;   // already advanced by k_face_rhs
+  const int64_t next_step = a.d_step[1];            // published by this step's k_face_rhs
+  const int64_t tt = next_step - 1 - a.d_step[2];   // source slot of the step being finished
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = e / a.W, w = e - j * a.W;
     // y = A^T J: a junction lies on one or two faces; the +-1 entries are sign flips
@@ -338,10 +355,11 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, Tables t, double* __
     }
     a.hout[e] = th;
     if (a.th_out && a.th_slot >= 0) a.th_out[a.th_slot * NjW + e] = th;
-    if (a.I_out && a.I_slot >= 0) a.I_out[a.I_slot * NjW + e] = y + view_at(a.Is, j, w);
-    if (a.theta_s && a.Vs.ptr) a.theta_s[e] += view_at(a.Vs, j, w) * a.dt;
-    if (kFuseNext) q[e] = junction_q(a, t, e, j, w, hist, next_step);
+    if (a.I_out && a.I_slot >= 0) a.I_out[a.I_slot * NjW + e] = y + view_at(a.Is, j, w, tt);
+    if (a.theta_s && a.Vs.ptr) a.theta_s[e] += view_at(a.Vs, j, w, tt) * a.dt;
+    if (kFuseNext) q[e] = junction_q(a, t, e, j, w, hist, next_step, tt + 1);
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.d_step[0] = next_step;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -651,12 +669,16 @@ struct jja_plan {
   int32_t* zrows_b = nullptr;   // rows of x accumulated by partial backward items
   int nz_f = 0, nz_b = 0;
   int64_t bytes = 0;
-  // cached graph of a fixed-length step sequence
-  cudaGraphExec_t gexec = nullptr;
-  int g_nsteps = 0;
-  std::vector<uint64_t> g_key;
+  // captured graphs of a fixed-length step sequence, keyed by the buffers they bake in (a few
+  // are kept: double-buffered source windows alternate between two keys), most recent last
+  struct CachedGraph {
+    std::vector<uint64_t> key;
+    cudaGraphExec_t exec;
+  };
+  std::vector<CachedGraph> graphs;
+  static constexpr size_t kMaxGraphs = 4;
   ~jja_plan() {
-    if (gexec) cudaGraphExecDestroy(gexec);
+    for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
     for (void* p : allocs) cudaFree(p);
   }
   template <class T>
@@ -735,14 +757,14 @@ StepArgs make_args(jja_plan* p, jja_state* s) {
   a.th_out = s->th_out;
   a.I_out = s->I_out;
   a.dt = p->dt;
-  a.Isq = s->Is.ptr ? jja_view{p->isq, p->W, 1} : jja_view{nullptr, 0, 0};
+  a.Isq = (s->Is.ptr && !s->Is.stride_t) ? jja_view{p->isq, p->W, 1, 0} : jja_view{nullptr, 0, 0, 0};
   a.resistive = p->resistive;
   return a;
 }
 
-// refresh Is / c0 from the state's current-source view (before the first step of a run)
+// refresh Is / c0 from a time-independent current-source view (before the first step of a run)
 void launch_scale_sources(jja_plan* p, jja_state* s, cudaStream_t st) {
-  if (!s->Is.ptr) return;
+  if (!s->Is.ptr || s->Is.stride_t) return;
   k_scale_sources<<<grid_for((int64_t)p->Nj * p->W, 256), 256, 0, st>>>(s->Is, p->t.inv_c0, p->isq, p->Nj, p->W);
   g_launches++;
 }
@@ -753,6 +775,65 @@ void rotate(jja_state* s, int width) {
   double* oldest = s->hist[nh - 1];
   for (int k = nh - 1; k > 0; --k) s->hist[k] = s->hist[k - 1];
   s->hist[0] = oldest;
+}
+
+// time-dependent sources must cover steps [step, step + nsteps)
+void check_window(const jja_state* s, int nsteps, const char* who) {
+  const jja_view* v[4] = {&s->Is, &s->f, &s->Vs, &s->T};
+  for (const jja_view* x : v) {
+    if (!x->ptr || !x->stride_t) continue;
+    if (s->step < s->src_t0 || s->step + nsteps > s->src_t0 + s->src_steps)
+      throw Error(JJA_ERR_ARG, std::string(who) + ": steps [" + std::to_string(s->step) + ", " +
+                                   std::to_string(s->step + nsteps) + ") are outside the source window [" +
+                                   std::to_string(s->src_t0) + ", " + std::to_string(s->src_t0 + s->src_steps) + ")");
+  }
+}
+
+void set_counters(jja_plan* p, const jja_state* s, cudaStream_t st) {
+  k_set_counters<<<1, 1, 0, st>>>(p->d_step, s->step, s->src_t0);
+  g_launches++;
+}
+
+// graph of G fused steps for the state's current buffers (captured on first use, then cached)
+cudaGraphExec_t graph_for(jja_plan* p, const jja_state* s, cudaStream_t st, int G) {
+  std::vector<uint64_t> key = {(uint64_t)s->hist[0], (uint64_t)s->hist[1], (uint64_t)s->hist[2],
+                               (uint64_t)s->hist[3], (uint64_t)s->theta_s, (uint64_t)s->noise_mode, s->seed,
+                               (uint64_t)st, (uint64_t)G};
+  for (const jja_view* v : {&s->Is, &s->f, &s->Vs, &s->T}) {
+    key.push_back((uint64_t)v->ptr);
+    key.push_back((uint64_t)v->stride_n);
+    key.push_back((uint64_t)v->stride_w);
+    key.push_back((uint64_t)v->stride_t);
+  }
+  for (size_t k = 0; k < p->graphs.size(); ++k) {
+    if (p->graphs[k].key != key) continue;
+    jja_plan::CachedGraph hit = p->graphs[k];
+    p->graphs.erase(p->graphs.begin() + k);
+    p->graphs.push_back(hit);
+    return hit.exec;
+  }
+  if (p->graphs.size() >= jja_plan::kMaxGraphs) {
+    cudaGraphExecDestroy(p->graphs.front().exec);
+    p->graphs.erase(p->graphs.begin());
+  }
+  const int period = p->width - 1;
+  cudaGraph_t g;
+  jja_state tmp = *s;
+  JJA_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  for (int q = 0; q < G; ++q) {
+    StepArgs a = make_args(p, &tmp);
+    a.hout = tmp.hist[period - 1];
+    a.th_slot = a.I_slot = -1;
+    launch_step(p, a, st, true);
+    rotate(&tmp, p->width);
+  }
+  JJA_CUDA(cudaStreamEndCapture(st, &g));
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) throw Error(JJA_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  p->graphs.push_back({key, exec});
+  return exec;
 }
 
 }  // namespace
@@ -1025,8 +1106,8 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->x = p->up<double>(nullptr, NfW);
     p->xj = p->up<double>(nullptr, NjW);
     p->isq = p->up<double>(nullptr, NjW);
-    p->d_step = p->up<int64_t>(nullptr, 1);
-    JJA_CUDA(cudaMemset(p->d_step, 0, sizeof(int64_t)));
+    p->d_step = p->up<int64_t>(nullptr, 3);
+    JJA_CUDA(cudaMemset(p->d_step, 0, 3 * sizeof(int64_t)));
     JJA_CUDA(cudaDeviceSynchronize());
     *out = p.release();
   });
@@ -1192,52 +1273,30 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
       if (!s->hist[k]) throw Error(JJA_ERR_ARG, "jja_run: missing history buffer");
     if (s->noise_mode == JJA_NOISE_BUFFER && !s->noise) throw Error(JJA_ERR_ARG, "jja_run: noise buffer missing");
     if (nsteps == 0) return;
+    check_window(s, nsteps, "jja_run");
     cudaStream_t st = (cudaStream_t)stream;
-    JJA_CUDA(cudaMemcpyAsync(p->d_step, &s->step, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    set_counters(p, s, st);
     launch_scale_sources(p, s, st);
     {
       StepArgs a = make_args(p, s);
       launch_junction(p, a, st);
     }
-    // one-step calls come from a host loop that changes sources between steps: no fusion
-    const bool fuse = nsteps > 1;
     const int period = p->width - 1;  // history rotation period
+    const int G = 16 * period;        // steps per captured graph: pointers return to their places
     int i = 0;
     while (i < nsteps) {
-      // a run of steps that store nothing can be replayed from a captured graph
+      // a run of steps that store nothing can be replayed from a captured graph; the call's
+      // last step stays out of it (it runs unfused: the look-ahead q it would evaluate belongs
+      // to a step outside this call, whose sources may lie outside the source window)
       int run = 0;
       while (i + run < nsteps && (!th_slot || th_slot[i + run] < 0) && (!I_slot || I_slot[i + run] < 0)) ++run;
-      const int G = 16 * period;
+      const int graphable = (i + run == nsteps) ? run - 1 : run;
       // capture needs a non-default stream; the per-step noise buffer is refilled by the host
-      if (use_graph && fuse && st != nullptr && run >= G && s->noise_mode != JJA_NOISE_BUFFER) {
-        std::vector<uint64_t> key = {(uint64_t)s->hist[0], (uint64_t)s->hist[1], (uint64_t)s->hist[2],
-                                     (uint64_t)s->hist[3], (uint64_t)s->theta_s, (uint64_t)s->Is.ptr,
-                                     (uint64_t)s->f.ptr, (uint64_t)s->Vs.ptr, (uint64_t)s->T.ptr,
-                                     (uint64_t)s->noise_mode, s->seed, (uint64_t)stream,
-                                     (uint64_t)s->Is.stride_n, (uint64_t)s->Is.stride_w,
-                                     (uint64_t)s->f.stride_n, (uint64_t)s->f.stride_w,
-                                     (uint64_t)s->T.stride_n, (uint64_t)s->T.stride_w,
-                                     (uint64_t)s->Vs.stride_n, (uint64_t)s->Vs.stride_w};
-        if (!p->gexec || p->g_key != key) {
-          if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
-          cudaGraph_t g;
-          jja_state tmp = *s;
-          JJA_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-          for (int q = 0; q < G; ++q) {
-            StepArgs a = make_args(p, &tmp);
-            a.hout = tmp.hist[period - 1];
-            a.th_slot = a.I_slot = -1;
-            launch_step(p, a, st, true);
-            rotate(&tmp, p->width);
-          }
-          JJA_CUDA(cudaStreamEndCapture(st, &g));
-          JJA_CUDA(cudaGraphInstantiate(&p->gexec, g, 0));
-          cudaGraphDestroy(g);
-          p->g_key = key;
-        }
-        const int reps = run / G;
-        for (int r = 0; r < reps; ++r) JJA_CUDA(cudaGraphLaunch(p->gexec, st));
-        i += reps * G;  // G is a multiple of the rotation period: pointers are unchanged
+      if (use_graph && st != nullptr && graphable >= G && s->noise_mode != JJA_NOISE_BUFFER) {
+        cudaGraphExec_t exec = graph_for(p, s, st, G);
+        const int reps = graphable / G;
+        for (int r = 0; r < reps; ++r) JJA_CUDA(cudaGraphLaunch(exec, st));
+        i += reps * G;
         run -= reps * G;
       }
       const int eager = (i < nsteps) ? std::max(run, 1) : 0;
@@ -1246,7 +1305,7 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
         a.hout = s->hist[period - 1];
         a.th_slot = th_slot ? th_slot[i] : -1;
         a.I_slot = I_slot ? I_slot[i] : -1;
-        launch_step(p, a, st, fuse);
+        launch_step(p, a, st, i + 1 < nsteps);
         rotate(s, p->width);
       }
     }
@@ -1259,8 +1318,9 @@ int jja_run_timed(jja_plan* p, jja_state* s, int nsteps, double* stage_ms, void*
   return guarded([&] {
     if (!p || !s || nsteps <= 0 || !stage_ms) throw Error(JJA_ERR_ARG, "jja_run_timed: bad arguments");
     if (s->noise_mode == JJA_NOISE_BUFFER) throw Error(JJA_ERR_ARG, "jja_run_timed: host noise buffer not supported");
+    check_window(s, nsteps, "jja_run_timed");
     cudaStream_t st = (cudaStream_t)stream;
-    JJA_CUDA(cudaMemcpyAsync(p->d_step, &s->step, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    set_counters(p, s, st);
     std::vector<cudaEvent_t> ev(1 + 5 * (size_t)nsteps);
     for (auto& e : ev) JJA_CUDA(cudaEventCreate(&e));
     JJA_CUDA(cudaEventRecord(ev[0], st));
@@ -1274,7 +1334,7 @@ int jja_run_timed(jja_plan* p, jja_state* s, int nsteps, double* stage_ms, void*
       StepArgs a = make_args(p, s);
       a.hout = s->hist[period - 1];
       a.th_slot = a.I_slot = -1;
-      launch_step(p, a, st, true, ev.data() + 1 + 5 * (size_t)i);
+      launch_step(p, a, st, i + 1 < nsteps, ev.data() + 1 + 5 * (size_t)i);
       rotate(s, p->width);
     }
     JJA_CUDA(cudaEventSynchronize(ev.back()));
