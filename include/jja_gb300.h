@@ -78,6 +78,27 @@ int jja_factor_solve_host(const jja_factor* f, double* b, int nrhs);
 
 /* ------------------------------------------------------------------------ GPU plan --- */
 
+/* Launch shape of the triangular-solve kernels; 0 in a field selects its default. The
+ * project's autotuner (pyjjasim_gb300/autotune.py) times candidates and picks these. */
+typedef struct {
+  int rhs_block;      /* problems per warp: a power of two <= 32 (default min(W, 32) rounded up) */
+  int rows_per_lane;  /* output rows per lane of a work item: 2, 4 or 8 (default 2) */
+  int target_warps;   /* levels with fewer work items split their dot products until they have
+                         this many (default 152 x 24) */
+  int min_piece;      /* shortest piece of a split dot product (default 16) */
+  int schedule;       /* 1: one launch per elimination-tree level; 2: dataflow, one persistent
+                         launch per sweep whose work items wait (bounded) on per-supernode
+                         completion counters; 0: default (1) */
+} jja_solve_tuning;
+
+/* Builds on the host (no GPU needed) the work-item schedule that jja_plan_create would make for
+ * W problems with `tuning` (NULL: defaults) and checks the dataflow order: every item waits only
+ * for items before it in its sweep, on counts equal to the items that will count. Returns
+ * JJA_ERR_INTERNAL when that fails (jja_plan_create makes the same check); the item counts of
+ * the two sweeps go to n_fwd_items / n_bwd_items (either may be NULL). */
+int jja_factor_check_schedule(const jja_factor* f, int W, const jja_solve_tuning* tuning, int64_t* n_fwd_items,
+                              int64_t* n_bwd_items);
+
 typedef struct {
   int Nj, Nf, W;           /* junctions, faces, problems per launch */
   int stencil_width;       /* 3, 4 or 5 (time_evolution.py:401-408) */
@@ -95,6 +116,7 @@ typedef struct {
   const double* Ic_w;      /* optional (Nj x W) critical currents per problem (replaces Ic): W
                               disorder realisations share one face-space matrix, since K does not
                               depend on Ic; NULL to use Ic for every problem */
+  jja_solve_tuning tuning; /* all zero: defaults */
 } jja_plan_desc;
 
 /* Uploads the circuit tables and the factor to the current CUDA device and allocates the
@@ -103,6 +125,15 @@ int jja_plan_create(const jja_plan_desc* desc, const jja_factor* f, jja_plan** o
 void jja_plan_destroy(jja_plan* p);
 /* Bytes of device memory held by the plan (tables + factor + work vectors). */
 int64_t jja_plan_device_bytes(const jja_plan* p);
+/* Synchronises the device, then reads and clears the plan's device error flag: *flow_timeouts
+ * = 1 if a wait of a dataflow sweep ran out of its bound since the last call (the results of
+ * those steps are invalid), else 0. */
+int jja_plan_check(jja_plan* p, int* flow_timeouts);
+/* Test of the bounded waits: runs one forward dataflow sweep whose wait counts can never be
+ * reached, then synchronises `stream`. Every wait gives up (the first after its bound, the rest
+ * at once), the kernel returns, and the plan's error flag is set for jja_plan_check to report.
+ * The plan's face-space work vectors hold garbage afterwards; the plan stays usable. */
+int jja_plan_test_wait_limit(jja_plan* p, void* stream);
 
 /* A source on the device: at step i, value(n, w) = ptr[n*stride_n + w*stride_w + (i - t0)*stride_t]
  * (element strides; 0 broadcasts). stride_t == 0: the same value at every step. stride_t != 0:

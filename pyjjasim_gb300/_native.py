@@ -28,11 +28,16 @@ class FactorStats(ctypes.Structure):
                 ("nnz_L", c_int64), ("f_values", c_int64), ("factor_flops", c_double)]
 
 
+class SolveTuning(ctypes.Structure):
+    _fields_ = [("rhs_block", c_int), ("rows_per_lane", c_int), ("target_warps", c_int), ("min_piece", c_int),
+                ("schedule", c_int)]
+
+
 class PlanDesc(ctypes.Structure):
     _fields_ = [("Nj", c_int), ("Nf", c_int), ("W", c_int), ("stencil_width", c_int),
                 ("a_rowptr", P_i64), ("a_col", P_i32), ("a_val", P_f64),
                 ("Ic", P_f64), ("inv_c0", P_f64), ("coef", P_f64), ("Rv", P_f64),
-                ("extrap", c_double * 4), ("dt", c_double), ("Ic_w", P_f64)]
+                ("extrap", c_double * 4), ("dt", c_double), ("Ic_w", P_f64), ("tuning", SolveTuning)]
 
 
 class View(ctypes.Structure):
@@ -60,9 +65,12 @@ SIGNATURES = {
     "jja_factor_get_perm": (c_int, [c_void_p, P_i32]),
     "jja_factor_get_supernodes": (c_int, [c_void_p, P_i32, P_i32, P_i32, P_i32, P_i32]),
     "jja_factor_solve_host": (c_int, [c_void_p, P_f64, c_int]),
+    "jja_factor_check_schedule": (c_int, [c_void_p, c_int, ctypes.POINTER(SolveTuning), P_i64, P_i64]),
     "jja_plan_create": (c_int, [ctypes.POINTER(PlanDesc), c_void_p, ctypes.POINTER(c_void_p)]),
     "jja_plan_destroy": (None, [c_void_p]),
     "jja_plan_device_bytes": (c_int64, [c_void_p]),
+    "jja_plan_check": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
+    "jja_plan_test_wait_limit": (c_int, [c_void_p, c_void_p]),
     "jja_run": (c_int, [c_void_p, ctypes.POINTER(State), c_int, P_i64, P_i64, c_int, c_void_p]),
     "jja_run_timed": (c_int, [c_void_p, ctypes.POINTER(State), c_int, P_f64, c_void_p]),
     "jja_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -159,9 +159,12 @@ class GpuSimulation:
     """
 
     def __init__(self, problem, noise="philox", seed=None, device=None, nd_leaf=8, stream=None, ordering="nd",
-                 relax=(-1, -1.0), Ic=None):
+                 relax=(-1, -1.0), Ic=None, tuning=None, tune=False):
         """``Ic``: optional (Nj, W) critical currents per problem, replacing the circuit's
-        (problems then differ in Ic but share the face-space matrix, which does not depend on Ic)."""
+        (problems then differ in Ic but share the face-space matrix, which does not depend on Ic).
+        ``tuning``: launch shape of the triangular solves (plan.TUNING_FIELDS); ``tune=True``
+        takes ``relax`` and ``tuning`` from the autotuner (timed once per GPU, circuit and W,
+        then cached on disk)."""
         torch = self.torch = _torch()
         c = problem.get_circuit()
         if not _is_default_cpr(problem.get_current_phase_relation()):
@@ -172,9 +175,15 @@ class GpuSimulation:
         self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.h2d_bytes = 0
         with torch.cuda.device(self.dev):
+            if tune:
+                from .autotune import autotune
+                opts = autotune(c, problem._dt(), self.W, self.width, nd_leaf=nd_leaf, device=self.dev.index)
+                ordering, relax, tuning = opts["ordering"], opts["relax"], opts["tuning"]
+            self.ordering = ordering
+            self.relax, self.tuning = tuple(relax), dict(tuning or {})
             self.stream = stream if stream is not None else torch.cuda.Stream(device=self.dev)
             self.plan = P.get_plan(c, problem._dt(), self.W, self.width, problem.stencil, nd_leaf=nd_leaf,
-                                   ordering=ordering, relax=relax, Ic_w=Ic)
+                                   ordering=ordering, relax=relax, Ic_w=Ic, tuning=tuning)
             hist0 = [problem.config_at_minus_1, problem.config_at_minus_2]
             if self.width >= 4:
                 hist0.append(problem.config_at_minus_3)
@@ -328,17 +337,21 @@ class GpuSimulation:
         raise RuntimeError("history buffer not found")
 
     def synchronize(self):
+        """Wait for the simulation's stream and check the plan's device error flag."""
         self.stream.synchronize()
+        self.plan.check()
 
 
 def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", seed=None, device=None,
-                        use_graph=True, nd_leaf=8, stream=None, ordering="nd", relax=(-1, -1.0), Ic=None):
+                        use_graph=True, nd_leaf=8, stream=None, ordering="nd", relax=(-1, -1.0), Ic=None,
+                        tuning=None, tune=False):
     """GPU time-stepping core; see the module docstring for the contract.
 
     ``ordering`` ("nd" or "mmd") and ``relax`` ((max zeros, max fraction) of supernode
-    amalgamation; negative = library defaults) select how the face-space matrix is factorised."""
+    amalgamation; negative = library defaults) select how the face-space matrix is factorised;
+    ``tuning`` the solve's launch shape; ``tune=True`` lets the autotuner pick both."""
     sim = GpuSimulation(problem, noise=noise, seed=seed, device=device, nd_leaf=nd_leaf, stream=stream,
-                        ordering=ordering, relax=relax, Ic=Ic)
+                        ordering=ordering, relax=relax, Ic=Ic, tuning=tuning, tune=tune)
     torch = sim.torch
     Nj, W, Nt, width = sim.Nj, sim.W, problem._Nt(), sim.width
     th_store_mask = np.asarray(th_store_mask, bool)
@@ -402,5 +415,6 @@ def solve_faces(circuit, dt, b, stencil_width=3, nd_leaf=8):
     st.synchronize()
     pl.solve(bd.data_ptr(), xd.data_ptr(), st.cuda_stream)
     st.synchronize()
+    pl.check()
     x = xd.cpu().numpy()
     return x[:, 0] if squeeze else x

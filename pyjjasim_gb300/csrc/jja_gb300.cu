@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -55,7 +56,9 @@ int guarded(F&& f) {
 }
 
 constexpr int kWarpsPerBlock = 4;   // level kernels: one warp per work item
-constexpr int kRowsPerLane = 4;     // rows of a work item handled by one lane
+constexpr int kDefaultRowsPerLane = 2;   // rows of a work item handled by one lane (2, 4 or 8)
+constexpr int kDefaultTargetWarps = 152 * 24;   // levels with fewer work items split their dot products
+constexpr int kDefaultMinPiece = 16;     // shortest piece of a split dot product
 constexpr int kUnroll = 4;          // columns whose loads are issued ahead of their FMAs
 constexpr double kTwoPi = 6.283185307179586;
 constexpr int kEllMax = 6;          // faces with up to 6 junctions (square 4, triangular 3, honeycomb 6)
@@ -157,19 +160,21 @@ __device__ __forceinline__ double signed_by(double v, int neg) {
 
 // ------------------------------------------------------------------------------------------
 // sin(x) in FP64 with few FP64 instructions (GB300's FP64 pipe is ~60x narrower than FP32).
-// Cody-Waite reduction x = k pi/2048 + t, |t| <= pi/4096, with pi/2048 = C1 + C2 + C3 where C1
-// and C2 carry 26 bits each (k C1 and k C2 are exact for |k| < 2^27); then
+// Cody-Waite reduction x = k pi/2048 + t, |t| <= pi/4096, with two constants: C1 = pi/2048
+// rounded to double, C2 = (pi/2048 - C1) rounded. fma(-k, C1, x) is exact for |k| < 2^27:
+// k C1 and x are multiples of 2^-63 there and their difference is below 2^-11, so it fits in
+// 52 bits; the second FMA adds one rounding of <= 2^-65 and the constants' own error is
+// < 2^-116 k. Then
 //   sin(x) = S + C t - S t^2/2 - C t^3/6 + S t^4/24 + O(t^5),  S, C = sin, cos(k pi/2048),
 // from a 4096-entry table computed on the host in extended precision. |t^3/6| < 7.6e-11 and
 // |t^4/24| < 1.5e-14, so those two terms are evaluated in FP32 (absolute error < 2e-17);
 // the rest is two FP64 FMAs (the table also holds -S/2). The O(t^5) remainder is below 3e-18.
 // |x| >= 2e5, inf and NaN fall back to the CUDA math library (range test on the integer pipe).
-// Nine FP64 instructions in all.
+// Eight FP64 instructions in all.
 // ------------------------------------------------------------------------------------------
 constexpr double kSinScale = 0x1.45f306dc9c883p+9;   // 2048 / pi
-constexpr double kSinC1 = 0x1.921fb58000000p-10;
-constexpr double kSinC2 = -0x1.dde9740000000p-37;
-constexpr double kSinC3 = 0x1.1a62633145c07p-64;
+constexpr double kSinC1 = 0x1.921fb54442d18p-10;     // pi/2048 rounded to double
+constexpr double kSinC2 = 0x1.1a62633145c07p-64;     // pi/2048 - kSinC1, rounded
 constexpr double kRoundMagic = 6755399441055744.0;   // 1.5 * 2^52: adding it rounds to an integer
 constexpr int kSinTable = 4096;
 
@@ -178,9 +183,7 @@ __device__ __forceinline__ double fast_sin(double x, const double2* __restrict__
   const double s = fma(x, kSinScale, kRoundMagic);
   const int k = __double2loint(s) & (kSinTable - 1);
   const double kd = s - kRoundMagic;
-  double t = fma(-kd, kSinC1, x);
-  t = fma(-kd, kSinC2, t);
-  t = fma(-kd, kSinC3, t);
+  const double t = fma(-kd, kSinC2, fma(-kd, kSinC1, x));
   const double2 sc = __ldg(tab + 2 * k);       // S, C
   const double2 hv = __ldg(tab + 2 * k + 1);   // -S/2, packed float S and C
   double r = fma(sc.y, t, sc.x);               // S + C t
@@ -201,9 +204,7 @@ __device__ __forceinline__ void fast_sincos(double x, const double2* __restrict_
   const double s = fma(x, kSinScale, kRoundMagic);
   const int k = __double2loint(s) & (kSinTable - 1);
   const double kd = s - kRoundMagic;
-  double t = fma(-kd, kSinC1, x);
-  t = fma(-kd, kSinC2, t);
-  t = fma(-kd, kSinC3, t);
+  const double t = fma(-kd, kSinC2, fma(-kd, kSinC1, x));
   const double2 sc = __ldg(tab + 2 * k);       // S, C
   const double2 hv = __ldg(tab + 2 * k + 1);   // -S/2, packed float S and C
   const double t2 = t * t;
@@ -388,13 +389,17 @@ __device__ __forceinline__ Item unpack_item(int4 v) {
   return it;
 }
 
-// zero the listed rows of an (Nf x W) vector before a sweep whose partial items accumulate there
-__global__ void k_zero_rows(double* __restrict__ v, const int32_t* __restrict__ rows, int n_rows, int W) {
+// zero the listed rows of an (Nf x W) vector before a sweep whose partial items accumulate
+// there, and the sweep's dataflow counters (n_ctr of them, none for level-synchronous sweeps)
+__global__ void k_zero_rows(double* __restrict__ v, const int32_t* __restrict__ rows, int n_rows, int W,
+                            unsigned* __restrict__ ctr, int n_ctr) {
   const int64_t n = (int64_t)n_rows * W;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = tid; e < n; e += nth) {
     const int64_t i = e / W, w = e - i * W;
     v[(int64_t)__ldg(rows + i) * W + w] = 0.0;
   }
+  for (int64_t e = tid; e < n_ctr; e += nth) ctr[e] = 0u;
 }
 
 struct FactorDev {
@@ -408,13 +413,12 @@ struct FactorDev {
   const double* frow;   // F_s row-major
 };
 
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, const int4* __restrict__ items,
-                                                                   int n_items, int W, int WB,
-                                                                   double* __restrict__ b, double* __restrict__ z) {
-  const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-  if (it >= n_items) return;
-  const int lane = threadIdx.x & 31;
-  const Item item = unpack_item(items[it]);
+// One forward work item (one warp): rows [r0, r1) of F_s b_s; diagonal rows go to z, the
+// off-diagonal rows are scattered (subtracted) into the ancestors' rows of b. b is read through
+// L2 (ld.global.cg): other warps of a dataflow sweep update it with atomics while this kernel runs.
+template <int kRowsPerLane>
+__device__ __forceinline__ void fwd_item(const FactorDev& F, const Item& item, int lane, int W, int WB,
+                                         double* __restrict__ b, double* __restrict__ z) {
   const int s = item.s, r0 = item.r0, r1 = item.r1, w0 = item.w0;
   const int LG = 32 / WB;
   const int w = w0 + lane % WB;
@@ -437,7 +441,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, 
   for (; j + kUnroll <= jend; j += kUnroll) {
     double bj[kUnroll], fv[kUnroll][kRowsPerLane];
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) bj[u] = b[(int64_t)(c0 + j + u) * W + w];
+    for (int u = 0; u < kUnroll; ++u) bj[u] = __ldcg(b + (int64_t)(c0 + j + u) * W + w);
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u)
 #pragma unroll
@@ -448,7 +452,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, 
       for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(fv[u][t], bj[u], acc[t]);
   }
   for (; j < jend; ++j) {
-    const double bj = b[(int64_t)(c0 + j) * W + w];
+    const double bj = __ldcg(b + (int64_t)(c0 + j) * W + w);
     const double* col = Fs + (int64_t)j * nf;
 #pragma unroll
     for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(__ldg(col + rr[t]), bj, acc[t]);
@@ -465,13 +469,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, 
   (void)m;
 }
 
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, const int4* __restrict__ items,
-                                                                   int n_items, int W, int WB,
-                                                                   const double* __restrict__ z, double* __restrict__ x) {
-  const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-  if (it >= n_items) return;
-  const int lane = threadIdx.x & 31;
-  const Item item = unpack_item(items[it]);
+// One backward work item: rows [i0, i1) of x_s = inv(L11)^T z_s - (L21 inv(L11))^T x[R_s].
+// x of the ancestors is read through L2 (written by other warps of a dataflow sweep).
+template <int kRowsPerLane>
+__device__ __forceinline__ void bwd_item(const FactorDev& F, const Item& item, int lane, int W, int WB,
+                                         const double* __restrict__ z, double* __restrict__ x) {
   const int s = item.s, i0 = item.r0, i1 = item.r1, w0 = item.w0;
   const int LG = 32 / WB;
   const int w = w0 + lane % WB;
@@ -524,14 +526,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
 #pragma unroll
       for (int t = 0; t < kRowsPerLane; ++t) fv[u][t] = __ldg(Fs + (int64_t)(k + q + u) * k + ii[t]);
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) xr[u] = x[(int64_t)idx[u] * W + w];
+    for (int u = 0; u < kUnroll; ++u) xr[u] = __ldcg(x + (int64_t)idx[u] * W + w);
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u)
 #pragma unroll
       for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(-fv[u][t], xr[u], acc[t]);
   }
   for (; q < q_end; ++q) {
-    const double xr = x[(int64_t)__ldg(R + q) * W + w];
+    const double xr = __ldcg(x + (int64_t)__ldg(R + q) * W + w);
     const double* row = Fs + (int64_t)(k + q) * k;
 #pragma unroll
     for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(-__ldg(row + ii[t]), xr, acc[t]);
@@ -544,6 +546,97 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
     else x[(int64_t)(c0 + i) * W + w] = acc[t];
   }
   (void)m;
+}
+
+// level-synchronous sweeps: one launch per elimination-tree level, one warp per item
+template <int kRowsPerLane>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, const int4* __restrict__ items,
+                                                                   int n_items, int W, int WB,
+                                                                   double* __restrict__ b, double* __restrict__ z) {
+  const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  if (it >= n_items) return;
+  fwd_item<kRowsPerLane>(F, unpack_item(items[it]), threadIdx.x & 31, W, WB, b, z);
+}
+
+template <int kRowsPerLane>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, const int4* __restrict__ items,
+                                                                   int n_items, int W, int WB,
+                                                                   const double* __restrict__ z, double* __restrict__ x) {
+  const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  if (it >= n_items) return;
+  bwd_item<kRowsPerLane>(F, unpack_item(items[it]), threadIdx.x & 31, W, WB, z, x);
+}
+
+// ------------------------------------------------------------------------------------------
+// Dataflow sweeps: ONE launch per sweep. Warps take items in the sweep's topological order from
+// a global counter; an item starts once the items it depends on have finished, which is
+// tracked by per-supernode completion counters instead of a kernel boundary per level:
+//   forward:  items of s wait until every item of s's children is done (children wait for
+//             theirs, so the whole subtree, which scatters into b_s, is done);
+//   backward: items of s wait until every item of s's parent is done (x of all ancestors).
+// No deadlock: a warp only waits for items earlier in the order, and every such item was taken
+// by a running warp before; the earliest unfinished item never waits. Every wait is bounded
+// (kFlowSpinLimit polls); a wait that runs out records an error flag that the host reads
+// (jja_plan_status), and the item then proceeds (its results are not to be used).
+// ------------------------------------------------------------------------------------------
+// polls of one wait (each a sleep of >= 64 ns plus an L2 round trip: 0.07-0.5 s in all), far
+// beyond the longest level of any plan (~ms); after one wait has run out, all others give up at once
+constexpr long long kFlowSpinLimit = 1LL << 20;
+
+struct Flow {
+  int* next;                    // item counter of this sweep (zeroed before the sweep)
+  unsigned* done;               // per-supernode completed-item counters (zeroed before the sweep)
+  const int32_t* wait_on;       // supernode whose counter an item of s waits on, or -1
+  const uint32_t* wait_count;   // ... until it reaches this count
+  const int32_t* notify;        // supernode whose counter an item of s increments when done, or -1
+  int* err;                     // set to 1 when a wait ran out
+};
+
+__device__ __forceinline__ void flow_wait(const Flow& fl, int s) {
+  const int t = __ldg(fl.wait_on + s);
+  if (t < 0) return;
+  const unsigned need = __ldg(fl.wait_count + s);
+  const volatile unsigned* c = fl.done + t;
+  const volatile int* err = fl.err;
+  for (long long i = 0; *c < need; ++i) {
+    if (i >= kFlowSpinLimit || *err) {
+      atomicExch(fl.err, 1);
+      return;
+    }
+    __nanosleep(64);
+  }
+  __threadfence();   // acquire: the producers' writes are visible before this item reads them
+}
+
+template <int kRowsPerLane, bool kForward>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_flow_sweep(FactorDev F, const int4* __restrict__ items,
+                                                                    int n_items, int W, int WB, double* b,
+                                                                    double* z, double* x, Flow fl) {
+  const int lane = threadIdx.x & 31;
+  // the next item is taken while the current one runs (hides the counter's round trip); a
+  // warp then holds two items, the later one not started, which keeps the order argument:
+  // the earliest unfinished item is always the one its warp is working on
+  int it = 0;
+  if (lane == 0) it = atomicAdd(fl.next, 1);
+  it = __shfl_sync(0xffffffffu, it, 0);
+  while (it < n_items) {
+    int nxt = 0;
+    if (lane == 0) nxt = atomicAdd(fl.next, 1);
+    const Item item = unpack_item(items[it]);
+    if (lane == 0) flow_wait(fl, item.s);
+    __syncwarp();
+    if (kForward) fwd_item<kRowsPerLane>(F, item, lane, W, WB, b, z);
+    else bwd_item<kRowsPerLane>(F, item, lane, W, WB, z, x);
+    __syncwarp();      // the warp's results, then one release fence and the completion count
+    if (lane == 0) {
+      const int t = __ldg(fl.notify + item.s);
+      if (t >= 0) {
+        __threadfence();
+        atomicAdd(fl.done + t, 1u);
+      }
+    }
+    it = __shfl_sync(0xffffffffu, nxt, 0);
+  }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -645,6 +738,161 @@ T* upload(const T* h, size_t n, int64_t& bytes) {
   return d;
 }
 
+// problems per warp of the triangular solves
+int resolve_rhs_block(int W, const jja_solve_tuning& tu) {
+  int WB = 1;
+  while (WB < std::min(W, 32)) WB <<= 1;
+  if (tu.rhs_block) {
+    if (tu.rhs_block < 1 || tu.rhs_block > 32 || (tu.rhs_block & (tu.rhs_block - 1)))
+      throw Error(JJA_ERR_ARG, "rhs_block must be a power of two <= 32");
+    WB = tu.rhs_block;
+  }
+  return WB;
+}
+
+// Work items of both sweeps and the dataflow dependencies, built on the host.
+struct Schedule {
+  int n_levels = 0, ns = 0;
+  std::vector<int4> fi;        // forward items, levels ascending (leaves first)
+  std::vector<int4> bi;        // backward items, levels ascending (level launches run them per level, root first)
+  std::vector<int4> bi_flow;   // the backward items root first (the dataflow sweep takes them in this order)
+  std::vector<int64_t> fwd_ptr, bwd_ptr;   // per level, into fi / bi
+  std::vector<int32_t> zf, zb;             // rows of z / x that partial items accumulate into
+  // forward: items of s wait until done[fon[s]] == fcnt[s] (fon[s] = s or -1) and then count
+  // towards fnot[s] (the parent); backward: items of s wait until done[bon[s]] == bcnt[s]
+  // (bon[s] = parent or -1) and count towards bnot[s] (s itself, if it has children)
+  std::vector<int32_t> fon, fnot, bon, bnot;
+  std::vector<uint32_t> fcnt, bcnt;
+};
+
+Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu) {
+  if (W <= 0 || W >= (1 << 30)) throw Error(JJA_ERR_ARG, "W must be in [1, 2^30)");
+  if (tu.rows_per_lane && tu.rows_per_lane != 2 && tu.rows_per_lane != 4 && tu.rows_per_lane != 8)
+    throw Error(JJA_ERR_ARG, "rows_per_lane must be 2, 4 or 8");
+  if (tu.target_warps < 0 || tu.min_piece < 0) throw Error(JJA_ERR_ARG, "target_warps and min_piece must be >= 0");
+  if (tu.schedule < 0 || tu.schedule > 2) throw Error(JJA_ERR_ARG, "schedule must be 0, 1 or 2");
+  const int WB = resolve_rhs_block(W, tu);
+  const int rpl = tu.rows_per_lane ? tu.rows_per_lane : kDefaultRowsPerLane;
+  const int target_warps = tu.target_warps ? tu.target_warps : kDefaultTargetWarps;
+  const int min_piece = tu.min_piece ? tu.min_piece : kDefaultMinPiece;
+  const int LG = 32 / WB, RPI = LG * rpl;
+  Schedule S;
+  S.n_levels = F.n_levels;
+  S.ns = F.ns;
+  std::vector<std::vector<int>> by_level(F.n_levels);
+  for (int s = 0; s < F.ns; ++s) {
+    if (F.sn_level[s] < 0 || F.sn_level[s] >= F.n_levels) throw Error(JJA_ERR_INTERNAL, "supernode level out of range");
+    by_level[F.sn_level[s]].push_back(s);
+    if (F.sn_k[s] + F.sn_m[s] >= 65536) throw Error(JJA_ERR_ARG, "supernode with >= 65536 rows");
+  }
+  auto pack = [](int s, int r0, int r1, int w0, bool partial, int c_lo, int c_hi) {
+    return make_int4(s, r0 | (r1 << 16), w0 | ((int)partial << 30), c_lo | (c_hi << 16));
+  };
+  // Levels with fewer items than can fill the GPU split each dot product into pieces of at
+  // least min_piece terms (multiples of the unroll), enough to reach target_warps warps.
+  const int nwc = (W + WB - 1) / WB;
+  auto pieces_of = [&](int len, int split) {
+    const int np = std::max(1, std::min(split, len / min_piece));
+    const int plen = ((len + np - 1) / np + kUnroll - 1) / kUnroll * kUnroll;
+    return std::max(plen, 1);
+  };
+  S.fwd_ptr.assign(1, 0);
+  S.bwd_ptr.assign(1, 0);
+  for (int l = 0; l < F.n_levels; ++l) {
+    int64_t nfw = 0, nbw = 0;
+    for (int s : by_level[l]) {
+      const int k = F.sn_k[s], nf = k + F.sn_m[s];
+      nfw += (int64_t)((nf + RPI - 1) / RPI) * nwc;
+      nbw += (int64_t)((k + RPI - 1) / RPI) * nwc;
+    }
+    const int fsplit = (int)std::max<int64_t>(1, (target_warps + nfw - 1) / std::max<int64_t>(nfw, 1));
+    const int bsplit = (int)std::max<int64_t>(1, (target_warps + nbw - 1) / std::max<int64_t>(nbw, 1));
+    for (int s : by_level[l]) {
+      const int k = F.sn_k[s], nf = k + F.sn_m[s], c0 = F.sn_col0[s];
+      bool zf_s = false, zb_s = false;
+      const int fplen = pieces_of(k, fsplit);
+      for (int r0 = 0; r0 < nf; r0 += RPI) {
+        const int r1 = std::min(nf, r0 + RPI), jmax = std::min(k, r1);
+        const bool partial = jmax > fplen;
+        zf_s |= partial && r0 < k;
+        for (int c_lo = 0; c_lo < jmax; c_lo += fplen)
+          for (int w0 = 0; w0 < W; w0 += WB)
+            S.fi.push_back(pack(s, r0, r1, w0, partial, c_lo, std::min(jmax, c_lo + fplen)));
+      }
+      for (int i0 = 0; i0 < k; i0 += RPI) {
+        const int i1 = std::min(k, i0 + RPI), len = nf - i0;
+        const int bplen = pieces_of(len, bsplit);
+        const bool partial = len > bplen;
+        zb_s |= partial;
+        for (int c_lo = i0; c_lo < nf; c_lo += bplen)
+          for (int w0 = 0; w0 < W; w0 += WB)
+            S.bi.push_back(pack(s, i0, i1, w0, partial, c_lo, std::min(nf, c_lo + bplen)));
+      }
+      if (zf_s) for (int i = 0; i < k; ++i) S.zf.push_back(c0 + i);
+      if (zb_s) for (int i = 0; i < k; ++i) S.zb.push_back(c0 + i);
+    }
+    S.fwd_ptr.push_back((int64_t)S.fi.size());
+    S.bwd_ptr.push_back((int64_t)S.bi.size());
+  }
+  for (int l = F.n_levels - 1; l >= 0; --l)
+    S.bi_flow.insert(S.bi_flow.end(), S.bi.begin() + S.bwd_ptr[l], S.bi.begin() + S.bwd_ptr[l + 1]);
+  const int ns = F.ns;
+  std::vector<uint32_t> nfi(ns, 0), nbi(ns, 0);
+  for (const int4& v : S.fi) nfi[v.x]++;
+  for (const int4& v : S.bi) nbi[v.x]++;
+  S.fcnt.assign(ns, 0);
+  S.bcnt.assign(ns, 0);
+  S.fon.assign(ns, -1);
+  S.fnot.assign(ns, -1);
+  S.bon.assign(ns, -1);
+  S.bnot.assign(ns, -1);
+  for (int s = 0; s < ns; ++s) {
+    const int par = F.sn_parent[s];
+    if (par < 0) continue;
+    if (par >= ns || F.sn_level[par] <= F.sn_level[s]) throw Error(JJA_ERR_INTERNAL, "supernode levels are not topological");
+    S.fcnt[par] += nfi[s];
+    S.fnot[s] = par;
+    S.bnot[par] = par;
+    S.bon[s] = par;
+    S.bcnt[s] = nbi[par];
+  }
+  for (int s = 0; s < ns; ++s)
+    if (S.fcnt[s]) S.fon[s] = s;
+  return S;
+}
+
+// Every item of a dataflow sweep may only wait for items that come before it in the sweep's
+// order, and the counts it waits for must be exactly the number of items that will count.
+// Otherwise warps could wait for items no running warp holds.
+void check_schedule(const Schedule& S) {
+  auto check = [&](const std::vector<int4>& items, const std::vector<int32_t>& on, const std::vector<uint32_t>& cnt,
+                   const std::vector<int32_t>& notify, const char* which) {
+    const int ns = S.ns;
+    std::vector<int64_t> first(ns, INT64_MAX), last_notifier(ns, -1);
+    std::vector<uint32_t> notifiers(ns, 0);
+    for (int64_t i = 0; i < (int64_t)items.size(); ++i) {
+      const int s = items[i].x;
+      if (s < 0 || s >= ns) throw Error(JJA_ERR_INTERNAL, std::string(which) + ": item supernode out of range");
+      first[s] = std::min(first[s], i);
+      const int t = notify[s];
+      if (t >= 0) {
+        last_notifier[t] = i;
+        notifiers[t]++;
+      }
+    }
+    for (int s = 0; s < ns; ++s) {
+      const int t = on[s];
+      if (t < 0) continue;
+      if (notifiers[t] != cnt[s])
+        throw Error(JJA_ERR_INTERNAL, std::string(which) + ": wait count does not match the items that count");
+      if (first[s] != INT64_MAX && last_notifier[t] >= first[s])
+        throw Error(JJA_ERR_INTERNAL, std::string(which) + ": an item waits for a later item");
+    }
+  };
+  check(S.fi, S.fon, S.fcnt, S.fnot, "forward schedule");
+  check(S.bi_flow, S.bon, S.bcnt, S.bnot, "backward schedule");
+}
+
 }  // namespace
 
 struct jja_factor {
@@ -652,14 +900,15 @@ struct jja_factor {
 };
 
 struct jja_plan {
-  int Nj = 0, Nf = 0, W = 0, width = 3, WB = 1, n_levels = 0;
+  int Nj = 0, Nf = 0, W = 0, width = 3, WB = 1, rows_per_lane = kDefaultRowsPerLane, n_levels = 0;
   double dt = 0.0, extrap[4] = {0, 0, 0, 0};
   Tables t{};
   FactorDev F{};
   std::vector<void*> allocs;
   std::vector<int64_t> fwd_ptr, bwd_ptr;
   int4* fwd_items = nullptr;
-  int4* bwd_items = nullptr;
+  int4* bwd_items = nullptr;        // levels ascending (level launches index them per level)
+  int4* bwd_flow_items = nullptr;   // the same items root first (dataflow sweep order)
   double *b = nullptr, *z = nullptr, *x = nullptr, *xj = nullptr;
   int32_t* perm = nullptr;   // new -> old face
   int64_t* d_step = nullptr;
@@ -668,6 +917,17 @@ struct jja_plan {
   int32_t* zrows_f = nullptr;   // rows of z accumulated by partial forward items
   int32_t* zrows_b = nullptr;   // rows of x accumulated by partial backward items
   int nz_f = 0, nz_b = 0;
+  // dataflow sweeps (schedule 2): dependency tables per supernode, counters, error flag
+  int flow = 0, ns = 0;
+  const int32_t* f_wait_on = nullptr;
+  const uint32_t* f_wait_count = nullptr;
+  const int32_t* f_notify = nullptr;
+  const int32_t* b_wait_on = nullptr;
+  const uint32_t* b_wait_count = nullptr;
+  const int32_t* b_notify = nullptr;
+  unsigned* counters = nullptr;   // forward: [next, done[ns]], then backward: [next, done[ns]]
+  int* flow_err = nullptr;
+  int flow_blocks[3][2] = {{0, 0}, {0, 0}, {0, 0}};   // resident blocks per (rows/lane 2,4,8) x (bwd, fwd)
   int64_t bytes = 0;
   // captured graphs of a fixed-length step sequence, keyed by the buffers they bake in (a few
   // are kept: double-buffered source windows alternate between two keys), most recent last
@@ -691,33 +951,78 @@ struct jja_plan {
 
 namespace {
 
-// zero the rows that partial items of the coming sweep accumulate into
+// zero the rows that partial items of the coming sweep accumulate into (and, for a dataflow
+// sweep, its counters)
 void launch_zero_rows(jja_plan* p, cudaStream_t st, bool forward, double* v) {
   const int n = forward ? p->nz_f : p->nz_b;
-  if (!n) return;
-  k_zero_rows<<<grid_for((int64_t)n * p->W, 256), 256, 0, st>>>(v, forward ? p->zrows_f : p->zrows_b, n, p->W);
+  const int n_ctr = p->flow ? p->ns + 1 : 0;
+  if (!n && !n_ctr) return;
+  unsigned* ctr = p->flow ? p->counters + (forward ? 0 : p->ns + 1) : nullptr;
+  k_zero_rows<<<grid_for(std::max<int64_t>((int64_t)n * p->W, n_ctr), 256), 256, 0, st>>>(
+      v, forward ? p->zrows_f : p->zrows_b, n, p->W, ctr, n_ctr);
   g_launches++;
 }
 
-void launch_levels(jja_plan* p, cudaStream_t st, bool forward) {
-  launch_zero_rows(p, st, forward, forward ? p->z : p->x);
+template <int RPL>
+void launch_flow(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x,
+                 const uint32_t* wait_count_override = nullptr) {
+  const int vi = RPL == 2 ? 0 : (RPL == 4 ? 1 : 2);   // index into flow_blocks
+  Flow fl;
+  unsigned* base = p->counters + (forward ? 0 : p->ns + 1);
+  fl.next = reinterpret_cast<int*>(base);
+  fl.done = base + 1;
+  fl.wait_on = forward ? p->f_wait_on : p->b_wait_on;
+  fl.wait_count = wait_count_override ? wait_count_override : (forward ? p->f_wait_count : p->b_wait_count);
+  fl.notify = forward ? p->f_notify : p->b_notify;
+  fl.err = p->flow_err;
+  const int n = (int)(forward ? p->fwd_ptr.back() : p->bwd_ptr.back());
+  if (!n) return;
+  const int grid = std::max(1, std::min((n + kWarpsPerBlock - 1) / kWarpsPerBlock, p->flow_blocks[vi][forward]));
+  if (forward)
+    k_flow_sweep<RPL, true><<<grid, kWarpsPerBlock * 32, 0, st>>>(p->F, p->fwd_items, n, p->W, p->WB, b, z, x, fl);
+  else
+    k_flow_sweep<RPL, false><<<grid, kWarpsPerBlock * 32, 0, st>>>(p->F, p->bwd_flow_items, n, p->W, p->WB, b, z, x,
+                                                                   fl);
+  g_launches++;
+}
+
+template <int RPL>
+void launch_sweep(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x) {
+  if (p->flow) {
+    launch_flow<RPL>(p, st, forward, b, z, x);
+    return;
+  }
   if (forward) {  // levels ascending (children before parents); b is consumed, z produced
     for (int l = 0; l < p->n_levels; ++l) {
       const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
       if (!n) continue;
-      k_fwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
-          p->F, p->fwd_items + p->fwd_ptr[l], n, p->W, p->WB, p->b, p->z);
+      k_fwd_level<RPL><<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
+          p->F, p->fwd_items + p->fwd_ptr[l], n, p->W, p->WB, b, z);
       g_launches++;
     }
   } else {        // levels descending; x produced
     for (int l = p->n_levels - 1; l >= 0; --l) {
       const int n = (int)(p->bwd_ptr[l + 1] - p->bwd_ptr[l]);
       if (!n) continue;
-      k_bwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
-          p->F, p->bwd_items + p->bwd_ptr[l], n, p->W, p->WB, p->z, p->x);
+      k_bwd_level<RPL><<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
+          p->F, p->bwd_items + p->bwd_ptr[l], n, p->W, p->WB, z, x);
       g_launches++;
     }
   }
+}
+
+// one triangular sweep over the levels with the plan's rows-per-lane variant of the kernels
+void launch_sweep_any(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x) {
+  switch (p->rows_per_lane) {
+    case 2: launch_sweep<2>(p, st, forward, b, z, x); break;
+    case 8: launch_sweep<8>(p, st, forward, b, z, x); break;
+    default: launch_sweep<4>(p, st, forward, b, z, x); break;
+  }
+}
+
+void launch_levels(jja_plan* p, cudaStream_t st, bool forward) {
+  launch_zero_rows(p, st, forward, forward ? p->z : p->x);
+  launch_sweep_any(p, st, forward, p->b, p->z, p->x);
 }
 
 // q of the first step of a run, from the phase history
@@ -910,6 +1215,19 @@ int jja_factor_solve_host(const jja_factor* f, double* b, int nrhs) {
   });
 }
 
+int jja_factor_check_schedule(const jja_factor* f, int W, const jja_solve_tuning* tuning, int64_t* n_fwd_items,
+                              int64_t* n_bwd_items) {
+  return guarded([&] {
+    if (!f) throw Error(JJA_ERR_ARG, "jja_factor_check_schedule: null factor");
+    jja_solve_tuning tu{};
+    if (tuning) tu = *tuning;
+    const Schedule S = build_schedule(*f->f, W, tu);
+    check_schedule(S);
+    if (n_fwd_items) *n_fwd_items = (int64_t)S.fi.size();
+    if (n_bwd_items) *n_bwd_items = (int64_t)S.bi_flow.size();
+  });
+}
+
 int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** out) {
   return guarded([&] {
     if (!d || !fac || !out) throw Error(JJA_ERR_ARG, "jja_plan_create: null argument");
@@ -920,9 +1238,11 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     std::unique_ptr<jja_plan> p(new jja_plan);
     p->Nj = d->Nj; p->Nf = d->Nf; p->W = d->W; p->width = d->stencil_width; p->dt = d->dt;
     for (int k = 0; k < 4; ++k) p->extrap[k] = d->extrap[k];
-    int WB = 1;
-    while (WB < std::min(d->W, 32)) WB <<= 1;
-    p->WB = WB;
+    // launch shape of the triangular solves (jja_solve_tuning; 0 = default), validated again
+    // by build_schedule
+    const jja_solve_tuning& tu = d->tuning;
+    p->WB = resolve_rhs_block(d->W, tu);
+    p->rows_per_lane = tu.rows_per_lane ? tu.rows_per_lane : kDefaultRowsPerLane;
     const int Nj = d->Nj, Nf = d->Nf;
     // face -> junction entries in the factor's face order; junction -> (<= 2) faces
     std::vector<int64_t> fj_ptr(Nf + 1, 0);
@@ -1033,73 +1353,46 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->F.valptr = p->up(F.sn_valptr.data(), F.sn_valptr.size());
     p->F.fcol = p->up(F.fcol.data(), F.fcol.size());
     p->F.frow = p->up(frow.data(), frow.size());
-    // work items per level
-    const int LG = 32 / WB, RPI = LG * kRowsPerLane;
-    p->n_levels = F.n_levels;
-    std::vector<std::vector<int>> by_level(F.n_levels);
-    for (int s = 0; s < F.ns; ++s) by_level[F.sn_level[s]].push_back(s);
-    if (d->W >= (1 << 30)) throw Error(JJA_ERR_ARG, "jja_plan_create: W too large");
-    for (int s = 0; s < F.ns; ++s)
-      if (F.sn_k[s] + F.sn_m[s] >= 65536) throw Error(JJA_ERR_ARG, "jja_plan_create: supernode with >= 65536 rows");
-    auto pack = [](int s, int r0, int r1, int w0, bool partial, int c_lo, int c_hi) {
-      return make_int4(s, r0 | (r1 << 16), w0 | ((int)partial << 30), c_lo | (c_hi << 16));
-    };
-    // Levels with fewer items than can fill the GPU split each dot product into pieces of at
-    // least kMinPiece terms (multiples of the unroll), enough to reach kTargetItems warps.
-    constexpr int kTargetItems = 152 * 24;
-    constexpr int kMinPiece = 16;
-    const int nwc = (d->W + WB - 1) / WB;
-    auto pieces_of = [&](int len, int split) {
-      const int np = std::max(1, std::min(split, len / kMinPiece));
-      const int plen = ((len + np - 1) / np + kUnroll - 1) / kUnroll * kUnroll;
-      return std::max(plen, 1);
-    };
-    std::vector<int4> fi, bi;
-    std::vector<int32_t> zf, zb;   // rows of z / x that partial items accumulate into
-    p->fwd_ptr.assign(1, 0);
-    p->bwd_ptr.assign(1, 0);
-    for (int l = 0; l < F.n_levels; ++l) {
-      int64_t nfw = 0, nbw = 0;
-      for (int s : by_level[l]) {
-        const int k = F.sn_k[s], nf = k + F.sn_m[s];
-        nfw += (int64_t)((nf + RPI - 1) / RPI) * nwc;
-        nbw += (int64_t)((k + RPI - 1) / RPI) * nwc;
-      }
-      const int fsplit = (int)std::max<int64_t>(1, (kTargetItems + nfw - 1) / std::max<int64_t>(nfw, 1));
-      const int bsplit = (int)std::max<int64_t>(1, (kTargetItems + nbw - 1) / std::max<int64_t>(nbw, 1));
-      for (int s : by_level[l]) {
-        const int k = F.sn_k[s], nf = k + F.sn_m[s], c0 = F.sn_col0[s];
-        bool zf_s = false, zb_s = false;
-        const int fplen = pieces_of(k, fsplit);
-        for (int r0 = 0; r0 < nf; r0 += RPI) {
-          const int r1 = std::min(nf, r0 + RPI), jmax = std::min(k, r1);
-          const bool partial = jmax > fplen;
-          zf_s |= partial && r0 < k;
-          for (int c_lo = 0; c_lo < jmax; c_lo += fplen)
-            for (int w0 = 0; w0 < d->W; w0 += WB)
-              fi.push_back(pack(s, r0, r1, w0, partial, c_lo, std::min(jmax, c_lo + fplen)));
+    // work items and dataflow dependencies (built and checked on the host)
+    const Schedule S = build_schedule(F, d->W, tu);
+    check_schedule(S);
+    p->n_levels = S.n_levels;
+    p->fwd_ptr = S.fwd_ptr;
+    p->bwd_ptr = S.bwd_ptr;
+    p->fwd_items = p->up(S.fi.data(), S.fi.size());
+    p->bwd_items = p->up(S.bi.data(), S.bi.size());
+    p->bwd_flow_items = p->up(S.bi_flow.data(), S.bi_flow.size());
+    p->nz_f = (int)S.zf.size();
+    p->nz_b = (int)S.zb.size();
+    p->zrows_f = p->up(S.zf.data(), S.zf.size());
+    p->zrows_b = p->up(S.zb.data(), S.zb.size());
+    {
+      const int ns = S.ns;
+      p->ns = ns;
+      p->f_wait_on = p->up(S.fon.data(), S.fon.size());
+      p->f_wait_count = p->up(S.fcnt.data(), S.fcnt.size());
+      p->f_notify = p->up(S.fnot.data(), S.fnot.size());
+      p->b_wait_on = p->up(S.bon.data(), S.bon.size());
+      p->b_wait_count = p->up(S.bcnt.data(), S.bcnt.size());
+      p->b_notify = p->up(S.bnot.data(), S.bnot.size());
+      p->counters = p->up<unsigned>(nullptr, 2 * ((size_t)ns + 1));
+      JJA_CUDA(cudaMemset(p->counters, 0, 2 * ((size_t)ns + 1) * sizeof(unsigned)));
+      p->flow_err = p->up<int>(nullptr, 1);
+      JJA_CUDA(cudaMemset(p->flow_err, 0, sizeof(int)));
+      int dev = 0, nsm = 0;
+      JJA_CUDA(cudaGetDevice(&dev));
+      JJA_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+      const void* kern[3][2] = {{(const void*)k_flow_sweep<2, false>, (const void*)k_flow_sweep<2, true>},
+                                {(const void*)k_flow_sweep<4, false>, (const void*)k_flow_sweep<4, true>},
+                                {(const void*)k_flow_sweep<8, false>, (const void*)k_flow_sweep<8, true>}};
+      for (int v = 0; v < 3; ++v)
+        for (int d = 0; d < 2; ++d) {
+          int occ = 0;
+          JJA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern[v][d], kWarpsPerBlock * 32, 0));
+          p->flow_blocks[v][d] = std::max(1, occ) * nsm;
         }
-        for (int i0 = 0; i0 < k; i0 += RPI) {
-          const int i1 = std::min(k, i0 + RPI), len = nf - i0;
-          const int bplen = pieces_of(len, bsplit);
-          const bool partial = len > bplen;
-          zb_s |= partial;
-          for (int c_lo = i0; c_lo < nf; c_lo += bplen)
-            for (int w0 = 0; w0 < d->W; w0 += WB)
-              bi.push_back(pack(s, i0, i1, w0, partial, c_lo, std::min(nf, c_lo + bplen)));
-        }
-        if (zf_s) for (int i = 0; i < k; ++i) zf.push_back(c0 + i);
-        if (zb_s) for (int i = 0; i < k; ++i) zb.push_back(c0 + i);
-      }
-      p->fwd_ptr.push_back((int64_t)fi.size());
-      p->bwd_ptr.push_back((int64_t)bi.size());
+      p->flow = (tu.schedule == 2) ? 1 : 0;
     }
-    p->fwd_items = p->up(fi.data(), fi.size());
-    p->bwd_items = p->up(bi.data(), bi.size());
-    p->nz_f = (int)zf.size();
-    p->nz_b = (int)zb.size();
-    p->zrows_f = p->up(zf.data(), zf.size());
-    p->zrows_b = p->up(zb.data(), zb.size());
     const size_t NfW = (size_t)Nf * d->W, NjW = (size_t)Nj * d->W;
     p->b = p->up<double>(nullptr, NfW);
     p->z = p->up<double>(nullptr, NfW);
@@ -1116,6 +1409,39 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
 void jja_plan_destroy(jja_plan* p) { delete p; }
 
 int64_t jja_plan_device_bytes(const jja_plan* p) { return p ? p->bytes : 0; }
+
+int jja_plan_test_wait_limit(jja_plan* p, void* stream) {
+  return guarded([&] {
+    if (!p) throw Error(JJA_ERR_ARG, "jja_plan_test_wait_limit: null plan");
+    cudaStream_t st = (cudaStream_t)stream;
+    const std::vector<uint32_t> never((size_t)std::max(p->ns, 1), 0xffffffffu);
+    uint32_t* d = nullptr;
+    JJA_CUDA(cudaMalloc(&d, never.size() * sizeof(uint32_t)));
+    const cudaError_t e1 = cudaMemcpy(d, never.data(), never.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e1 == cudaSuccess) {
+      const int saved = p->flow;
+      p->flow = 1;
+      launch_zero_rows(p, st, true, p->z);
+      launch_flow<kDefaultRowsPerLane>(p, st, true, p->b, p->z, p->x, d);
+      p->flow = saved;
+    }
+    const cudaError_t e2 = cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (e1 != cudaSuccess) throw Error(JJA_ERR_CUDA, cudaGetErrorString(e1));
+    if (e2 != cudaSuccess) throw Error(JJA_ERR_CUDA, cudaGetErrorString(e2));
+  });
+}
+
+int jja_plan_check(jja_plan* p, int* flow_timeouts) {
+  return guarded([&] {
+    if (!p || !flow_timeouts) throw Error(JJA_ERR_ARG, "jja_plan_check: null argument");
+    JJA_CUDA(cudaDeviceSynchronize());
+    int h = 0;
+    JJA_CUDA(cudaMemcpy(&h, p->flow_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) JJA_CUDA(cudaMemset(p->flow_err, 0, sizeof(int)));
+    *flow_timeouts = h;
+  });
+}
 
 int jja_solve(jja_plan* p, const double* b, double* x, void* stream) {
   return guarded([&] {
@@ -1165,23 +1491,7 @@ double* static_scratch_for_current_device() {
 // the level sweeps of launch_levels with explicit work vectors
 void launch_levels_into(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x) {
   launch_zero_rows(p, st, forward, forward ? z : x);
-  if (forward) {
-    for (int l = 0; l < p->n_levels; ++l) {
-      const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
-      if (!n) continue;
-      k_fwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
-          p->F, p->fwd_items + p->fwd_ptr[l], n, p->W, p->WB, b, z);
-      g_launches++;
-    }
-  } else {
-    for (int l = p->n_levels - 1; l >= 0; --l) {
-      const int n = (int)(p->bwd_ptr[l + 1] - p->bwd_ptr[l]);
-      if (!n) continue;
-      k_bwd_level<<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
-          p->F, p->bwd_items + p->bwd_ptr[l], n, p->W, p->WB, z, x);
-      g_launches++;
-    }
-  }
+  launch_sweep_any(p, st, forward, b, z, x);
 }
 
 }  // namespace

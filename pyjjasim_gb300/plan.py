@@ -24,6 +24,9 @@ MAX_PLANS = 4
 
 # Extrapolation weights of the CPR argument on theta(t-1), theta(t-2), ... (time_evolution.py:547-553)
 EXTRAP = {3: (2.0, -1.0), 4: (3.0, -3.0, 1.0), 5: (4.0, -6.0, 4.0, -1.0)}
+# launch-shape fields of the triangular solves (jja_solve_tuning)
+TUNING_FIELDS = ("rhs_block", "rows_per_lane", "target_warps", "min_piece", "schedule")
+SCHEDULES = {"levels": 1, "dataflow": 2}
 
 
 def _digest(*arrays):
@@ -96,6 +99,16 @@ class HostFactor:
                                                                 for k in ("col0", "k", "m", "level", "parent"))))
         return out
 
+    def check_schedule(self, W, tuning=None):
+        """Build the GPU work-item schedule for W problems on the host and check its dataflow
+        order (raises JJAError otherwise); returns the item counts (forward, backward)."""
+        t = dict(tuning or {})
+        tu = N.SolveTuning(*(int(t.get(f, 0)) for f in TUNING_FIELDS))
+        nf, nb = ctypes.c_int64(0), ctypes.c_int64(0)
+        N.check(N.lib().jja_factor_check_schedule(self.handle, int(W), ctypes.byref(tu), ctypes.byref(nf),
+                                                  ctypes.byref(nb)))
+        return nf.value, nb.value
+
     def solve_host(self, b):
         """Host solve (diagnostic). b: (n,) or (n, nrhs)."""
         b = np.array(b, dtype=np.float64, order="C", copy=True)
@@ -113,7 +126,9 @@ class HostFactor:
 class DevicePlan:
     """Circuit tables + factor uploaded for W problems (owned C object)."""
 
-    def __init__(self, circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=None):
+    def __init__(self, circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=None, tuning=None):
+        """``tuning``: dict with any of rhs_block, rows_per_lane, target_warps, min_piece (the
+        launch shape of the triangular solves; missing or 0 = library default)."""
         Nj, Nf = circuit._Nj(), circuit._Nf()
         Rv, Cv, coef = coefficients(circuit, dt, stencil)
         Acsr = scipy.sparse.csr_matrix(A)
@@ -132,6 +147,12 @@ class DevicePlan:
         d = N.PlanDesc(Nj, Nf, W, stencil_width, N.ptr(k["rowptr"], ctypes.c_int64), N.ptr(k["col"], ctypes.c_int32),
                        N.ptr(k["val"]), N.ptr(k["Ic"]), N.ptr(k["inv_c0"]), N.ptr(k["coef"]), N.ptr(k["Rv"]), ex, dt,
                        N.ptr(k["Ic_w"]))
+        tuning = dict(tuning or {})
+        unknown = set(tuning) - set(TUNING_FIELDS)
+        if unknown:
+            raise ValueError(f"unknown tuning fields {sorted(unknown)}; expected {TUNING_FIELDS}")
+        d.tuning = N.SolveTuning(*(int(tuning.get(f, 0)) for f in TUNING_FIELDS))
+        self.tuning = {f: int(tuning.get(f, 0)) for f in TUNING_FIELDS}
         h = ctypes.c_void_p()
         N.check(N.lib().jja_plan_create(ctypes.byref(d), factor.handle, ctypes.byref(h)))
         self.handle = h
@@ -141,6 +162,14 @@ class DevicePlan:
 
     def solve(self, b_dev, x_dev, stream=0):
         N.check(N.lib().jja_solve(self.handle, ctypes.c_void_p(b_dev), ctypes.c_void_p(x_dev), ctypes.c_void_p(stream)))
+
+    def check(self):
+        """Synchronise the device; raise JJAError if a wait of a dataflow sweep ran out of its
+        bound since the last check (the steps since then are invalid)."""
+        t = ctypes.c_int(0)
+        N.check(N.lib().jja_plan_check(self.handle, ctypes.byref(t)))
+        if t.value:
+            raise N.JJAError(5, "a dataflow sweep's dependency wait ran out of its bound; results are invalid")
 
     def eval_sin(self, x_dev, out_dev, n, stream=0):
         N.check(N.lib().jja_eval_sin(self.handle, ctypes.c_void_p(x_dev), ctypes.c_void_p(out_dev), int(n),
@@ -191,17 +220,20 @@ def get_factor(circuit, dt, nd_leaf=8, ordering="nd", relax=(-1, -1.0)):
     return _FACTORS[key][0], A, key
 
 
-def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=8, ordering="nd", relax=(-1, -1.0), Ic_w=None):
-    """Device plan for W problems; ``Ic_w`` (Nj, W) gives each problem its own critical currents."""
+def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=8, ordering="nd", relax=(-1, -1.0), Ic_w=None,
+             tuning=None):
+    """Device plan for W problems; ``Ic_w`` (Nj, W) gives each problem its own critical currents;
+    ``tuning`` the launch shape of the triangular solves (see DevicePlan)."""
     factor, A, fkey = get_factor(circuit, dt, nd_leaf, ordering=ordering, relax=relax)
     Rv, Cv, coef = coefficients(circuit, dt, stencil)
     if Ic_w is not None:
         Ic_w = np.ascontiguousarray(np.broadcast_to(np.asarray(Ic_w, np.float64), (circuit._Nj(), W)))
     ic = np.asarray(circuit._Ic(), np.float64) if Ic_w is None else Ic_w
-    key = (fkey, W, stencil_width, Ic_w is None, _digest(ic, *coef, Rv, A.indptr, A.indices, A.data))
+    tkey = tuple(int((tuning or {}).get(f, 0)) for f in TUNING_FIELDS)
+    key = (fkey, W, stencil_width, Ic_w is None, tkey, _digest(ic, *coef, Rv, A.indptr, A.indices, A.data))
     p = _PLANS.get(key)
     if p is None:
-        p = DevicePlan(circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=Ic_w)
+        p = DevicePlan(circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=Ic_w, tuning=tuning)
         _PLANS[key] = p
         while len(_PLANS) > MAX_PLANS:
             _PLANS.popitem(last=False)

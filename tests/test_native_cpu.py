@@ -96,3 +96,22 @@ def test_plan_create_without_gpu_reports_cuda_error():
     with pytest.raises(N.JJAError) as e:
         P.DevicePlan(c, f, A, 2, 0.05, 3, ((1.0, -1.0, 0.0), (1.0, -2.0, 1.0)))
     assert e.value.code == 3  # JJA_ERR_CUDA
+
+
+@pytest.mark.parametrize("make", [lambda: SquareArray(128, 128), lambda: HoneycombArray(20, 17),
+                                  lambda: TriangularArray(30, 21), lambda: SquareArray(7, 5)])
+@pytest.mark.parametrize("ordering", ["nd", "mmd"])
+@pytest.mark.parametrize("W,tuning", [(1, None), (8, {"rows_per_lane": 8}), (64, {"rhs_block": 16}),
+                                      (512, None), (512, {"rows_per_lane": 2, "min_piece": 4,
+                                                          "target_warps": 152 * 200}), (3, {"schedule": 2})])
+def test_dataflow_schedule_waits_only_on_earlier_items(make, ordering, W, tuning):
+    """The work-item schedule of both sweeps (built on the host exactly as the GPU plan builds it)
+    is a valid dataflow order: no item waits for a later item, and every wait count equals the
+    number of items that count towards it. A violation could make warps wait for items no
+    running warp holds."""
+    c = make()
+    A, K = P.face_matrix(c, 0.05)
+    coords, perm = P.fill_reducing_order(K, ordering, c)
+    f = P.HostFactor(K, coords=coords, perm=perm)
+    nf, nb = f.check_schedule(W, tuning)
+    assert nf >= f.stats["n_supernodes"] and nb >= f.stats["n_supernodes"]
