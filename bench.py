@@ -185,6 +185,128 @@ def adjoint_leg(G, torch, Nt):
             "mean_loss": float(run.loss.mean().item())}
 
 
+def _timed_steps(torch, sim, steps):
+    """Device seconds of `steps` graph-replayed steps (after one graph's warm-up)."""
+    sim.run(16 * (sim.width - 1) + 1, use_graph=True)
+    sim.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(sim.stream)
+    sim.run(steps, use_graph=True)
+    e1.record(sim.stream)
+    e1.synchronize()
+    sim.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def ac_driven_leg(G, torch, Nt, parity_steps=200):
+    """The AC-driven single array: SquareArray(256,256), beta_C = 1 (C = 1 with R = Ic = 1),
+    self-inductance 0.1, f = 0.1, bias current_base(0) x (0.8 + 0.3 sin(2 pi 0.05 t)) given as a
+    callable of the step, T = 0.01 with on-device Philox noise, dt = 0.05, W = 1. Timed end to
+    end through compute() (the callable is evaluated on the host for every step, in windows
+    uploaded while the GPU runs). Parity: `parity_steps` steps with the reference's noise
+    draws replayed (noise="numpy") against the oracle."""
+    from oracle import rcsj_oracle
+    n, dt = 256, 0.05
+    a = G.SquareArray(n, n)
+    a.set_capacitance(1.0)
+    a.set_inductance(0.1)
+    base = a.current_base(0.0)[:, None]     # (Nj, 1): the problem axis the reference broadcasts to
+
+    def Is(i):
+        return base * (0.8 + 0.3 * np.sin(2 * np.pi * 0.05 * i * dt))
+
+    def problem(steps, store):
+        return G.TimeEvolutionProblem(a, time_step=dt, time_step_count=steps, current_sources=Is, external_flux=0.1,
+                                      temperature=0.01, store_time_steps=store, store_current=False)
+
+    problem(64, [63]).compute(seed=1)                 # plan, graphs
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = problem(Nt, [Nt - 1]).compute(seed=2)
+    V = res.get_voltage()
+    t = time.perf_counter() - t0
+    Nj = a._Nj()
+    out = {"workload": f"SquareArray(256,256), C=1, L=0.1, f=0.1, Is(i) = current_base(0) (0.8 + 0.3 sin(2 pi 0.05 i dt)) "
+                       f"(callable), T=0.01 (Philox), dt=0.05, W=1, {Nt} steps",
+           "Nj": Nj, "steps": Nt, "seconds": t, "value": Nj * Nt / t, "unit": "junction-steps/s",
+           "timing": "end to end through compute(), host callable evaluated per step inside the timed region",
+           "finite": bool(np.isfinite(V).all())}
+    if parity_steps:
+        po = problem(parity_steps, [parity_steps - 2, parity_steps - 1])
+        np.random.seed(11)
+        rg = po.compute(noise="numpy")
+        np.random.seed(11)
+        th_o, _, V_o = rcsj_oracle.time_evolution(po)
+        out["parity"] = {"steps": parity_steps, "noise": "the reference's np.random draws replayed on the GPU",
+                         "max_abs_theta_error": float(np.abs(rg.get_theta() - th_o).max()),
+                         "max_abs_voltage_error": float(np.abs(rg.get_voltage() - V_o).max())}
+    return out
+
+
+def large_array_leg(G, torch, steps):
+    """The large single array: SquareArray(1024,1024) (2.1M junctions), beta_C = 0.5, L = 0.05,
+    f = 0.1, 8 DC bias values 0.5-1.2 in one batch, T = 0.005 with on-device Philox noise,
+    dt = 0.05. The bias pattern is unit current on the horizontal junctions, which is what
+    current_base(0) gives for a square array up to ~1e-14 (its node-space solve alone takes
+    ~17 s at this size). `steps` graph-replayed steps are timed with CUDA events."""
+    from pyjjasim_gb300.backend import GpuSimulation
+    n = 1024
+    t0 = time.perf_counter()
+    a = G.SquareArray(n, n)
+    a.set_capacitance(0.5)
+    a.set_inductance(0.05)
+    base = np.concatenate([np.ones(n * (n - 1)), np.zeros(n * (n - 1))])
+    bias = np.linspace(0.5, 1.2, 8)
+    p = G.TimeEvolutionProblem(a, time_step=0.05, time_step_count=10000,
+                               current_sources=base[:, None, None] * bias[None, :, None], external_flux=0.1,
+                               temperature=0.005, store_time_steps=[9999])
+    sim = GpuSimulation(p, seed=3)
+    sim.synchronize()
+    t_plan = time.perf_counter() - t0
+    el = _timed_steps(torch, sim, steps)
+    Nj, W = a._Nj(), 8
+    from pyjjasim_gb300 import plan as P
+    fstats = list(P._FACTORS.values())[-1][0].stats if P._FACTORS else None   # the most recent factor
+    return {"workload": "SquareArray(1024,1024), C=0.5, L=0.05, f=0.1, bias linspace(0.5,1.2,8) on the horizontal "
+                        "junctions, T=0.005 (Philox), dt=0.05, W=8",
+            "Nj": Nj, "W": W, "steps": steps, "ms_per_step": el / steps * 1e3, "value": Nj * W * steps / el,
+            "unit": "junction-steps/s", "setup_seconds": t_plan, "device_bytes": int(sim.plan.device_bytes),
+            "factor": {k: fstats[k] for k in ("nnz_L", "n_levels", "max_k")} if fstats else None,
+            "finite": bool(torch.isfinite(sim.theta()).all())}
+
+
+def ragged_leg(G, torch, n_problems, steps):
+    """The ragged batch: problems drawn (seeded) with lattice type uniform over square /
+    honeycomb / triangular and side n ~ U{32..256}, bias linspace(0, 2, 256)[k] on
+    current_base(0) of problem k, f = 0.25, T = 0, dt = 0.05; the first `n_problems` of the 256
+    draws run as one block-diagonal system. `steps` graph-replayed steps timed with CUDA events."""
+    from pyjjasim_gb300.backend import GpuSimulation
+    from pyjjasim_gb300.ragged import RaggedBatch
+    rng = np.random.default_rng(7)
+    kinds, sizes = rng.integers(0, 3, 256), rng.integers(32, 257, 256)
+    bias = np.linspace(0.0, 2.0, 256)
+    lattices = (G.SquareArray, G.HoneycombArray, G.TriangularArray)
+    t0 = time.perf_counter()
+    probs = []
+    for k, nn, b in list(zip(kinds, sizes, bias))[:n_problems]:
+        c = lattices[k](int(nn), int(nn))
+        probs.append(G.TimeEvolutionProblem(c, time_step=0.05, time_step_count=steps + 64,
+                                            current_sources=c.current_base(0.0)[:, None, None] * b,
+                                            external_flux=0.25, store_time_steps=[steps + 63]))
+    rb = RaggedBatch(probs)
+    sim = GpuSimulation(rb.union_problem())
+    sim.synchronize()
+    t_setup = time.perf_counter() - t0
+    el = _timed_steps(torch, sim, steps)
+    return {"workload": f"ragged: first {n_problems} of 256 seeded problems (square/honeycomb/triangular, side "
+                        f"32-256), f=0.25, bias linspace(0,2,256), T=0, dt=0.05, one block-diagonal system",
+            "problems": n_problems, "Nj_total": rb.Nj, "Nf_total": rb.Nf, "steps": steps,
+            "ms_per_step": el / steps * 1e3, "value": rb.Nj * steps / el, "unit": "junction-steps/s",
+            "setup_seconds": t_setup, "finite": bool(torch.isfinite(sim.theta()).all()),
+            "lattices": [[["square", "honeycomb", "triangular"][int(k)], int(nn)]
+                         for k, nn in list(zip(kinds, sizes))[:n_problems]]}
+
+
 PARITY_PROBLEMS = (150, 250, 350, 450)   # bias 0.59, 0.98, 1.37, 1.76: across the IV curve
 
 
@@ -353,6 +475,11 @@ def main():
                     help="time steps of the end-to-end compute() call (the workload's 10000)")
     ap.add_argument("--parity-steps", type=int, default=1000,
                     help="time steps of the oracle comparison on four of the problems (0 skips it)")
+    ap.add_argument("--ac-steps", type=int, default=20000, help="steps of the AC-driven 256x256 leg (0 skips it)")
+    ap.add_argument("--large-steps", type=int, default=300, help="timed steps of the 1024x1024 leg (0 skips it)")
+    ap.add_argument("--ragged-problems", type=int, default=32,
+                    help="problems of the ragged leg, the first of 256 seeded draws (0 skips it)")
+    ap.add_argument("--ragged-steps", type=int, default=200, help="timed steps of the ragged leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -509,6 +636,22 @@ def main():
                                   "host inside the timed region, results (theta, I, V) back on the host"}
         if args.parity_steps > 0:
             line["parity"] = parity_leg(G, args.parity_steps)
+        # the other configurations of the workload family, each guarded so that one failing
+        # leg reports its error instead of losing the line
+        others = {}
+        for name, fn in (("ac_driven_256x256", lambda: ac_driven_leg(G, torch, args.ac_steps)),
+                         ("single_1024x1024_w8", lambda: large_array_leg(G, torch, args.large_steps)),
+                         ("ragged", lambda: ragged_leg(G, torch, args.ragged_problems, args.ragged_steps))):
+            if (name.startswith("ac") and args.ac_steps <= 0) or (name.startswith("single") and args.large_steps <= 0) \
+                    or (name == "ragged" and args.ragged_problems <= 0):
+                continue
+            try:
+                others[name] = fn()
+            except Exception as e:      # report, keep the headline line
+                others[name] = {"error": f"{type(e).__name__}: {e}"}
+            torch.cuda.empty_cache()
+        if others:
+            line["other_configs"] = others
         if args.adjoint_steps > 0:
             line["adjoint"] = adjoint_leg(G, torch, args.adjoint_steps)
         if not args.no_cpu_baseline:
