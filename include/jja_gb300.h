@@ -228,6 +228,13 @@ int jja_solve(jja_plan* p, const double* b, double* x, void* stream);
  * b and x are caller-owned device arrays (Nf x W, original face order), as for jja_solve. */
 int jja_solve_static(jja_plan* p, const double* b, double* x, void* stream);
 
+/* Vortex configurations of n_steps stored phase arrays theta (device, n_steps x Nj x W):
+ * n_s(f, w) = -sum_j A_fj round(theta_s(j, w) / 2 pi) (TimeEvolutionResult.get_vortex_configuration,
+ * time_evolution.py:734-755), written to n_out (device n_steps x Nf x W int32, original face
+ * order) when not NULL; and flow[w] += sum_f sum_{s>=1} |n_s(f,w) - n_{s-1}(f,w)| (device W
+ * uint64; the numerator of AnnealingProblem's vortex mobility, :1131-1136) when not NULL. */
+int jja_vortex(jja_plan* p, const double* theta, int64_t n_steps, int32_t* n_out, uint64_t* flow, void* stream);
+
 /* out[i] = sin(x[i]) with the library's device sine (device arrays of n doubles), the one
  * the junction-current kernels use for Ic sin(theta) (pyjjasim static_problem.py:82-85).
  * Exposed so tests can bound its error against a correctly rounded sine. */

@@ -198,3 +198,52 @@ def vortex_configuration(A, theta):
     Nj, W, S = theta.shape
     r = np.round(theta / (2.0 * np.pi)).reshape(Nj, W * S)
     return (-(A @ r)).reshape(Nf, W, S).astype(int)
+
+
+def anneal(problem_cls, circuit, time_step=0.5, interval_steps=10, external_flux=0.0, current_sources=0,
+           problem_count=1, interval_count=1000, vortex_mobility=0.001, start_T=1.0, T_factor=1.03):
+    """Restatement of AnnealingProblem.compute (time_evolution.py:1070-1191) up to, not including,
+    its final static (Newton) refinement, with the noise of ``evolve`` (np.random, per call).
+
+    ``problem_cls``: a TimeEvolutionProblem class with the reference's constructor and attributes
+    (the reference's own or a mirror of it). Follows the reference literally: each interval
+    restarts from config_at_minus_1 = config_at_minus_2 = the last phase; the vortex mobility is
+    sum |diff n| / (Nf dt (interval_count - 1)) (:1131-1136); the temperature of a problem is
+    divided by T_factor when its mobility exceeds the target v ((N - i) / N)^1.5, else multiplied
+    (:1138-1143); then five runs at T = 0 with half the time step (:1171-1178).
+    Returns (theta (Nj, W), vortex configuration (Nf, W) at the last step, temperature profiles
+    (interval_count, W), vortex mobility (interval_count, W)).
+    """
+    Nj, Nf = circuit._Nj(), circuit._Nf()
+    W = problem_count
+    T = start_T * np.ones((1, W, 1))
+    f = np.atleast_1d(external_flux)[:, None, None]
+    th = np.zeros((Nj, W))
+    prob = problem_cls(circuit, time_step_count=interval_steps, time_step=time_step, external_flux=f,
+                       current_sources=current_sources, temperature=T, store_current=False, store_voltage=False,
+                       stencil_width=3)
+    A = circuit.get_cycle_matrix()
+    profiles = np.zeros((interval_count, W))
+    mobility = np.zeros((interval_count, W))
+    for i in range(interval_count):
+        prob.temperature = T * np.ones((1, 1, interval_steps))
+        prob.config_at_minus_1 = th
+        prob.config_at_minus_2 = th.copy()
+        theta, _, _ = time_evolution(prob)
+        n = vortex_configuration(A, theta)
+        mob = np.sum(np.sum(np.abs(np.diff(n, axis=2)), axis=2), axis=0) / (Nf * time_step * (interval_count - 1))
+        v = vortex_mobility
+        upper = v[i] if np.array(v).size == interval_count else v * ((interval_count - i) / interval_count) ** 1.5
+        factor = (mob > upper) * (1 / T_factor) + (mob <= upper) * T_factor
+        T = T * factor[..., None]
+        th = theta[..., -1]
+        profiles[i] = T[0, :, 0]
+        mobility[i] = mob
+    prob.temperature = np.zeros((1, 1, interval_steps))
+    prob.time_step /= 2
+    for _ in range(5):
+        prob.config_at_minus_1 = th
+        prob.config_at_minus_2 = th.copy()
+        theta, _, _ = time_evolution(prob)
+        th = theta[..., -1]
+    return th, vortex_configuration(A, theta)[:, :, -1], profiles, mobility

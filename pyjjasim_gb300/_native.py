@@ -77,6 +77,7 @@ SIGNATURES = {
     "jja_solve_static": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "jja_adjoint_step": (c_int, [c_void_p, ctypes.POINTER(AdjointArgs), c_void_p]),
     "jja_adjoint_flux": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "jja_vortex": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "jja_eval_sin": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
     "jja_last_error": (ctypes.c_char_p, []),
     "jja_launch_count": (c_int64, []),

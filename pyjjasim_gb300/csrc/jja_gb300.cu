@@ -697,6 +697,36 @@ __global__ void __launch_bounds__(256) k_adj_mu(AdjArgs a, Tables t, const doubl
   }
 }
 
+// Vortex configurations n_s(f, w) = -sum_j A_fj round(theta_s(j, w) / 2 pi) of n_steps stored
+// phase arrays (time_evolution.py:734-755; np.round is round-half-even, as rint), written in
+// the original face order when n_out is given, and the vortex flow per problem,
+// flow[w] += sum_f sum_{s >= 1} |n_s - n_{s-1}| (the numerator of AnnealingProblem's vortex
+// mobility, time_evolution.py:1131-1136), when flow is given. One thread per (face, problem).
+__global__ void __launch_bounds__(256) k_vortex(const double* __restrict__ theta, int64_t n_steps, int Nj, int Nf,
+                                                int W, Tables t, int32_t* __restrict__ n_out,
+                                                unsigned long long* __restrict__ flow) {
+  const int64_t NfW = (int64_t)Nf * W, NjW = (int64_t)Nj * W;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NfW; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = e / W, w = e - p * W;
+    const int64_t i0 = __ldg(t.fj_ptr + p), i1 = __ldg(t.fj_ptr + p + 1);
+    const int64_t fo = __ldg(t.face_orig + p);
+    long long prev = 0, moved = 0;
+    for (int64_t s = 0; s < n_steps; ++s) {
+      const double* th = theta + s * NjW;
+      long long n = 0;
+      for (int64_t i = i0; i < i1; ++i) {
+        const int code = __ldg(t.fj_col + i);          // (junction << 1) | (A entry is -1)
+        const long long r = (long long)rint(th[(int64_t)(code >> 1) * W + w] / kTwoPi);
+        n += (code & 1) ? r : -r;                      // n = -A round(theta / 2 pi)
+      }
+      if (n_out) n_out[s * NfW + fo * W + w] = (int32_t)n;
+      if (s > 0) moved += n > prev ? n - prev : prev - n;
+      prev = n;
+    }
+    if (flow && moved) atomicAdd(flow + w, (unsigned long long)moved);
+  }
+}
+
 __global__ void k_unpermute_scaled(const double* __restrict__ src, double* __restrict__ dst,
                                    const int32_t* __restrict__ perm, int n, int W, double scale) {
   const int64_t nW = (int64_t)n * W;
@@ -1560,6 +1590,18 @@ int jja_adjoint_flux(jja_plan* p, const double* usum, double* gf, void* stream) 
     launch_levels(p, st, true);
     launch_levels(p, st, false);
     k_unpermute_scaled<<<grid_for(NfW, 256), 256, 0, st>>>(p->x, gf, p->perm, p->Nf, p->W, -kTwoPi);
+    g_launches++;
+    JJA_CUDA(cudaGetLastError());
+  });
+}
+
+int jja_vortex(jja_plan* p, const double* theta, int64_t n_steps, int32_t* n_out, uint64_t* flow, void* stream) {
+  return guarded([&] {
+    if (!p || !theta || n_steps < 0) throw Error(JJA_ERR_ARG, "jja_vortex: bad arguments");
+    if (!n_steps || (!n_out && !flow)) return;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_vortex<<<grid_for((int64_t)p->Nf * p->W, 256), 256, 0, st>>>(theta, n_steps, p->Nj, p->Nf, p->W, p->t, n_out,
+                                                                    reinterpret_cast<unsigned long long*>(flow));
     g_launches++;
     JJA_CUDA(cudaGetLastError());
   });

@@ -107,6 +107,33 @@ def run_case(pj, name, circuit, dt, Nt, *, f=0.0, Is=0.0, Vs=0.0, T=0.0, seed=No
           f"{os.path.getsize(path) / 1024:.0f} KB")
 
 
+def anneal_case(pj, name, circuit, seed, **params):
+    """Run the reference AnnealingProblem.compute() and save its inputs, the temperature profiles
+    and the vortex configurations it hands to its final static refinement (recorded by wrapping
+    TimeEvolutionProblem.get_static_problem at run time; the reference's files are untouched)."""
+    handed = []
+    orig = pj.TimeEvolutionProblem.get_static_problem
+
+    def record(self, vortex_configuration, *a, **k):
+        handed.append(np.array(vortex_configuration, dtype=np.int64))
+        return orig(self, vortex_configuration, *a, **k)
+
+    pj.TimeEvolutionProblem.get_static_problem = record
+    try:
+        np.random.seed(seed)
+        status, configs, profiles = pj.AnnealingProblem(circuit, **params).compute()
+    finally:
+        pj.TimeEvolutionProblem.get_static_problem = orig
+    d = circuit_parts(circuit)
+    d.update(seed=np.int64(seed), temperature_profiles=profiles, status=np.asarray(status),
+             final_vortex=np.stack(handed, axis=1))
+    for k, v in params.items():
+        d["param_" + k] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+    print(f"{name}: Nj={circuit.junction_count()} W={params.get('problem_count', 1)} "
+          f"intervals={params.get('interval_count')}")
+
+
 def every(Nt, k):
     m = np.zeros(Nt, bool)
     m[::k] = True
@@ -117,8 +144,11 @@ def every(Nt, k):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--anneal-only", action="store_true", help="write only the AnnealingProblem fixtures")
     args = ap.parse_args()
     pj = import_reference(args.ref)
+    if args.anneal_only:
+        return anneal_fixtures(pj)
 
     # Lattice fixtures: cycle matrices, cut matrices and current_base for the three lattice kinds.
     lat = {}
@@ -212,6 +242,15 @@ def main():
     th2 = th1 - 0.01
     run_case(pj, "c10_square7x5_timedep", a, 0.1, Nt, f=fa, Is=Is[:, None, None], T=Ta, seed=9,
              store=every(Nt, 3), th_m1=th1, th_m2=th2)
+    anneal_fixtures(pj)
+
+
+def anneal_fixtures(pj):
+    # AnnealingProblem (time_evolution.py:1070-1191): per-problem temperatures driven by the
+    # measured vortex mobility (they diverge between problems with these parameters)
+    anneal_case(pj, "a1_square6x5_anneal", pj.SquareArray(6, 5), 5, time_step=0.5, interval_steps=8,
+                interval_count=40, problem_count=3, external_flux=0.25, vortex_mobility=0.05, start_T=1.0,
+                T_factor=1.1)
 
 
 if __name__ == "__main__":
