@@ -89,6 +89,9 @@ typedef struct {
   int schedule;       /* 1: one launch per elimination-tree level; 2: dataflow, one persistent
                          launch per sweep whose work items wait (bounded) on per-supernode
                          completion counters; 0: default (1) */
+  int pdl;            /* 1: launch the step's kernels with programmatic dependent launch (each
+                         launch overlaps the tail of the kernel before; measured: 6 % faster for
+                         W = 1, 5-7 % slower for W >= 64); 0: default (plain launches) */
 } jja_solve_tuning;
 
 /* Builds on the host (no GPU needed) the work-item schedule that jja_plan_create would make for

@@ -5,6 +5,8 @@ GPU depends on choices that have no single best value across array sizes and bat
 
 * ``schedule``: one launch per elimination-tree level, or one persistent dataflow launch per
   sweep whose work items wait on per-supernode completion counters (no gaps between levels);
+* ``pdl``: programmatic dependent launch of the step's kernels (launch latency hidden behind
+  the previous kernel's tail; pays off when the kernels are short);
 * ``ordering``: nested dissection (shallow tree, big supernodes) or minimum degree (about 30 %
   less fill on 2-D arrays, but a deeper tree of smaller supernodes);
 * ``relax``: how far supernodes are amalgamated (fewer, wider supernodes and fewer elimination-
@@ -33,10 +35,10 @@ from . import plan as P
 
 CACHE_ENV = "PYJJASIM_GB300_TUNE_CACHE"
 DEFAULT = {"schedule": 1, "ordering": "nd", "relax": (-1, -1.0), "rows_per_lane": 2, "rhs_block": 0,
-           "target_warps": 152 * 24}
+           "target_warps": 152 * 24, "pdl": 0}
 # searched in this order; a tuple is searched jointly (ordering and rows per lane interact:
 # minimum degree's smaller supernodes want fewer rows per warp)
-AXES = (("ordering", "rows_per_lane"), "schedule", "rhs_block", "target_warps", "relax")
+AXES = (("ordering", "rows_per_lane"), "schedule", "pdl", "rhs_block", "target_warps", "relax")
 
 
 def cache_path():
@@ -56,6 +58,7 @@ def candidates(W):
     wb = default_rhs_block(W)
     return {
         "schedule": [1, 2],
+        "pdl": [0, 1],
         "ordering": ["nd", "mmd"],
         "rows_per_lane": [2, 4, 8],
         "rhs_block": [0] + [b for b in (wb // 2, wb // 4) if b >= 1],
@@ -68,7 +71,8 @@ def to_options(cfg):
     """GpuSimulation options of a configuration."""
     return {"ordering": str(cfg["ordering"]), "relax": tuple(cfg["relax"]),
             "tuning": {"rows_per_lane": int(cfg["rows_per_lane"]), "rhs_block": int(cfg["rhs_block"]),
-                       "target_warps": int(cfg["target_warps"]), "schedule": int(cfg["schedule"])}}
+                       "target_warps": int(cfg["target_warps"]), "schedule": int(cfg["schedule"]),
+                       "pdl": int(cfg.get("pdl", 0))}}
 
 
 def coordinate_descent(W, measure, min_gain=0.02):

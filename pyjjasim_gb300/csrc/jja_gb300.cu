@@ -91,6 +91,15 @@ __device__ __forceinline__ double philox_normal(uint64_t seed, uint64_t elem, ui
   return (double)(rad * cospif(2.0f * u2));
 }
 
+// Programmatic dependent launch: every kernel first lets the next kernel of its stream be
+// scheduled (once all of its own blocks have started), then waits until the previous kernel
+// has finished and its writes are visible. The dependent launch overlaps the ~us gap between
+// the many short kernels of a step; both instructions are no-ops for plain launches.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // value of a source at (n, w) in time slot tt = step - window start (ignored when stride_t == 0)
 __device__ __forceinline__ double view_at(const jja_view& v, int64_t n, int64_t w, int64_t tt = 0) {
   return v.ptr ? __ldg(v.ptr + n * v.stride_n + w * v.stride_w + tt * v.stride_t) : 0.0;
@@ -132,7 +141,7 @@ struct Tables {
   const int32_t* fj_ell;   // faces of <= kEllMax junctions: Nf x face_deg codes, padded with -1
   int face_deg;            // 0 when some face has more than kEllMax junctions (CSR path)
   const int32_t* jf_face;  // 2 per junction: (permuted face << 1) | (A entry is -1), or -1
-  const double2* sincos;   // per k < 4096: {S, C}, {-S/2, (float S, float C)}; S, C = sin, cos(k pi/2048)
+  const double2* sincos;   // per k < 65536: {S, C} = {sin, cos}(k pi/32768)
 };
 
 // FP64 <-> FP32 conversions by bit manipulation on the integer pipe: on GB300 the conversion
@@ -160,23 +169,23 @@ __device__ __forceinline__ double signed_by(double v, int neg) {
 
 // ------------------------------------------------------------------------------------------
 // sin(x) in FP64 with few FP64 instructions (GB300's FP64 pipe is ~60x narrower than FP32).
-// Cody-Waite reduction x = k pi/2048 + t, |t| <= pi/4096, with two constants: C1 = pi/2048
-// rounded to double, C2 = (pi/2048 - C1) rounded. fma(-k, C1, x) is exact for |k| < 2^27:
-// k C1 and x are multiples of 2^-63 there and their difference is below 2^-11, so it fits in
-// 52 bits; the second FMA adds one rounding of <= 2^-65 and the constants' own error is
-// < 2^-116 k. Then
-//   sin(x) = S + C t - S t^2/2 - C t^3/6 + S t^4/24 + O(t^5),  S, C = sin, cos(k pi/2048),
-// from a 4096-entry table computed on the host in extended precision. |t^3/6| < 7.6e-11 and
-// |t^4/24| < 1.5e-14, so those two terms are evaluated in FP32 (absolute error < 2e-17);
-// the rest is two FP64 FMAs (the table also holds -S/2). The O(t^5) remainder is below 3e-18.
-// |x| >= 2e5, inf and NaN fall back to the CUDA math library (range test on the integer pipe).
-// Eight FP64 instructions in all.
+// Cody-Waite reduction x = k pi/32768 + t, |t| <= pi/65536 = 4.8e-5, with two constants:
+// C1 = pi/32768 rounded to double, C2 = (pi/32768 - C1) rounded. fma(-k, C1, x) is exact for
+// |x| < 2e5: k C1 and x are multiples of 2^-67 there and their difference is below 2^-14, so it
+// fits in 52 bits; the second FMA adds one rounding of <= 2^-69 and the constants' own error
+// is < 2^-120 k. Then
+//   sin(x) = S + C t - S t^2/2 - C t^3/6 + O(t^4),  S, C = sin, cos(k pi/32768),
+// from a 65536-entry table (1 MB, L2-resident) computed on the host in extended precision.
+// |S t^2/2| < 1.2e-9 and |t^3/6| < 1.9e-14, so both terms are evaluated in FP32 (absolute
+// error < 1e-16, checked by exact emulation and on the GPU); S + C t is one FP64 FMA and the
+// O(t^4) remainder is below 3e-19. |x| >= 2e5, inf and NaN fall back to the CUDA math library
+// (range test on the integer pipe). Six FP64 instructions in all.
 // ------------------------------------------------------------------------------------------
-constexpr double kSinScale = 0x1.45f306dc9c883p+9;   // 2048 / pi
-constexpr double kSinC1 = 0x1.921fb54442d18p-10;     // pi/2048 rounded to double
-constexpr double kSinC2 = 0x1.1a62633145c07p-64;     // pi/2048 - kSinC1, rounded
+constexpr double kSinScale = 0x1.45f306dc9c883p+13;  // 32768 / pi
+constexpr double kSinC1 = 0x1.921fb54442d18p-14;     // pi/32768 rounded to double
+constexpr double kSinC2 = 0x1.1a62633145c07p-68;     // pi/32768 - kSinC1, rounded
 constexpr double kRoundMagic = 6755399441055744.0;   // 1.5 * 2^52: adding it rounds to an integer
-constexpr int kSinTable = 4096;
+constexpr int kSinTable = 65536;
 
 __device__ __forceinline__ double fast_sin(double x, const double2* __restrict__ tab) {
   if ((__double2hiint(x) & 0x7fffffff) >= 0x41086A00) return sin(x);   // |x| >= 2e5, inf, NaN
@@ -184,18 +193,15 @@ __device__ __forceinline__ double fast_sin(double x, const double2* __restrict__
   const int k = __double2loint(s) & (kSinTable - 1);
   const double kd = s - kRoundMagic;
   const double t = fma(-kd, kSinC2, fma(-kd, kSinC1, x));
-  const double2 sc = __ldg(tab + 2 * k);       // S, C
-  const double2 hv = __ldg(tab + 2 * k + 1);   // -S/2, packed float S and C
-  double r = fma(sc.y, t, sc.x);               // S + C t
-  r = fma(hv.x, t * t, r);                     // - S t^2/2
-  const float sf = __int_as_float(__double2loint(hv.y)), cf = __int_as_float(__double2hiint(hv.y));
-  const float tf = f32_from_f64(t);
+  const double2 sc = __ldg(tab + k);           // S, C
+  const double r = fma(sc.y, t, sc.x);         // S + C t
+  const float tf = f32_from_f64(t), sf = f32_from_f64(sc.x), cf = f32_from_f64(sc.y);
   const float t2 = tf * tf;
-  const float tail = fmaf(sf * (1.0f / 24.0f), t2 * t2, -(cf * (1.0f / 6.0f)) * (t2 * tf));
+  const float tail = fmaf(-0.5f * sf, t2, (-(1.0f / 6.0f) * cf) * (t2 * tf));   // -S t^2/2 - C t^3/6
   return r + f64_from_f32(tail);
 }
 
-// sin and cos from one reduction: cos(a + t) = C - S t - C t^2/2 + S t^3/6 + C t^4/24 + O(t^5)
+// sin and cos from one reduction: cos(a + t) = C - S t - C t^2/2 + S t^3/6 + O(t^4)
 __device__ __forceinline__ void fast_sincos(double x, const double2* __restrict__ tab, double& s_out, double& c_out) {
   if ((__double2hiint(x) & 0x7fffffff) >= 0x41086A00) {
     sincos(x, &s_out, &c_out);
@@ -205,18 +211,13 @@ __device__ __forceinline__ void fast_sincos(double x, const double2* __restrict_
   const int k = __double2loint(s) & (kSinTable - 1);
   const double kd = s - kRoundMagic;
   const double t = fma(-kd, kSinC2, fma(-kd, kSinC1, x));
-  const double2 sc = __ldg(tab + 2 * k);       // S, C
-  const double2 hv = __ldg(tab + 2 * k + 1);   // -S/2, packed float S and C
-  const double t2 = t * t;
-  double rs = fma(sc.y, t, sc.x);              // S + C t
-  rs = fma(hv.x, t2, rs);                      // - S t^2/2
-  double rc = fma(-sc.x, t, sc.y);             // C - S t
-  rc = fma(-0.5 * sc.y, t2, rc);               // - C t^2/2
-  const float sf = __int_as_float(__double2loint(hv.y)), cf = __int_as_float(__double2hiint(hv.y));
-  const float tf = f32_from_f64(t);
-  const float tf2 = tf * tf, tf3 = tf2 * tf, tf4 = tf2 * tf2;
-  const float ts = fmaf(sf * (1.0f / 24.0f), tf4, -(cf * (1.0f / 6.0f)) * tf3);
-  const float tc = fmaf(cf * (1.0f / 24.0f), tf4, (sf * (1.0f / 6.0f)) * tf3);
+  const double2 sc = __ldg(tab + k);           // S, C
+  const double rs = fma(sc.y, t, sc.x);        // S + C t
+  const double rc = fma(-sc.x, t, sc.y);       // C - S t
+  const float tf = f32_from_f64(t), sf = f32_from_f64(sc.x), cf = f32_from_f64(sc.y);
+  const float t2 = tf * tf, t3 = t2 * tf;
+  const float ts = fmaf(-0.5f * sf, t2, (-(1.0f / 6.0f) * cf) * t3);
+  const float tc = fmaf(-0.5f * cf, t2, ((1.0f / 6.0f) * sf) * t3);
   s_out = rs + f64_from_f32(ts);
   c_out = rc + f64_from_f32(tc);
 }
@@ -262,6 +263,7 @@ __device__ __forceinline__ double junction_q(const StepArgs& a, const Tables& t,
 // Isq = Is / c0 per junction, refreshed at the start of every run (and every host-driven step)
 __global__ void __launch_bounds__(256) k_scale_sources(jja_view Is, const double* __restrict__ inv_c0,
                                                        double* __restrict__ Isq, int Nj, int W) {
+  pdl_begin();
   const int64_t NjW = (int64_t)Nj * W;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = e / W, w = e - j * W;
@@ -271,6 +273,7 @@ __global__ void __launch_bounds__(256) k_scale_sources(jja_view Is, const double
 
 // q for the first step of a run, from the stored phase history
 __global__ void __launch_bounds__(256) k_junction(StepArgs a, Tables t, double* __restrict__ q) {
+  pdl_begin();
   const int64_t NjW = (int64_t)a.Nj * a.W;
   const int64_t step = a.d_step[0], tt = step - a.d_step[2];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
@@ -285,6 +288,7 @@ __global__ void __launch_bounds__(256) k_junction(StepArgs a, Tables t, double* 
 // the step counters at the start of a call (kernel arguments are fixed at launch, so the
 // host's values need no pinned staging)
 __global__ void k_set_counters(int64_t* __restrict__ d_step, int64_t step, int64_t t0) {
+  pdl_begin();
   d_step[0] = step;
   d_step[1] = step;
   d_step[2] = t0;
@@ -294,6 +298,7 @@ __global__ void k_set_counters(int64_t* __restrict__ d_step, int64_t step, int64
 // publishes step + 1 in d_step[1] (read by k_update, which evaluates the next step's q).
 __global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const double* __restrict__ q,
                                                   double* __restrict__ b) {
+  pdl_begin();
   const int64_t NfW = (int64_t)a.Nf * a.W;
   const int64_t step = a.d_step[0], tt = step - a.d_step[2];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NfW; e += (int64_t)gridDim.x * blockDim.x) {
@@ -338,6 +343,7 @@ __global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const do
 template <bool kFuseNext>
 __global__ void __launch_bounds__(256) k_update(StepArgs a, Tables t, double* __restrict__ q,
                                                 const double* __restrict__ J) {
+  pdl_begin();
   const int64_t NjW = (int64_t)a.Nj * a.W;
   const int64_t next_step = a.d_step[1];            // published by this step's k_face_rhs
   const int64_t tt = next_step - 1 - a.d_step[2];   // source slot of the step being finished
@@ -393,6 +399,7 @@ __device__ __forceinline__ Item unpack_item(int4 v) {
 // there, and the sweep's dataflow counters (n_ctr of them, none for level-synchronous sweeps)
 __global__ void k_zero_rows(double* __restrict__ v, const int32_t* __restrict__ rows, int n_rows, int W,
                             unsigned* __restrict__ ctr, int n_ctr) {
+  pdl_begin();
   const int64_t n = (int64_t)n_rows * W;
   const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
   for (int64_t e = tid; e < n; e += nth) {
@@ -553,6 +560,7 @@ template <int kRowsPerLane>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, const int4* __restrict__ items,
                                                                    int n_items, int W, int WB,
                                                                    double* __restrict__ b, double* __restrict__ z) {
+  pdl_begin();
   const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (it >= n_items) return;
   fwd_item<kRowsPerLane>(F, unpack_item(items[it]), threadIdx.x & 31, W, WB, b, z);
@@ -562,6 +570,7 @@ template <int kRowsPerLane>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, const int4* __restrict__ items,
                                                                    int n_items, int W, int WB,
                                                                    const double* __restrict__ z, double* __restrict__ x) {
+  pdl_begin();
   const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (it >= n_items) return;
   bwd_item<kRowsPerLane>(F, unpack_item(items[it]), threadIdx.x & 31, W, WB, z, x);
@@ -612,6 +621,7 @@ template <int kRowsPerLane, bool kForward>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_flow_sweep(FactorDev F, const int4* __restrict__ items,
                                                                     int n_items, int W, int WB, double* b,
                                                                     double* z, double* x, Flow fl) {
+  pdl_begin();
   const int lane = threadIdx.x & 31;
   // the next item is taken while the current one runs (hides the counter's round trip); a
   // warp then holds two items, the later one not started, which keeps the order argument:
@@ -801,6 +811,7 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu)
     throw Error(JJA_ERR_ARG, "rows_per_lane must be 2, 4 or 8");
   if (tu.target_warps < 0 || tu.min_piece < 0) throw Error(JJA_ERR_ARG, "target_warps and min_piece must be >= 0");
   if (tu.schedule < 0 || tu.schedule > 2) throw Error(JJA_ERR_ARG, "schedule must be 0, 1 or 2");
+  if (tu.pdl < 0 || tu.pdl > 1) throw Error(JJA_ERR_ARG, "pdl must be 0 or 1");
   const int WB = resolve_rhs_block(W, tu);
   const int rpl = tu.rows_per_lane ? tu.rows_per_lane : kDefaultRowsPerLane;
   const int target_warps = tu.target_warps ? tu.target_warps : kDefaultTargetWarps;
@@ -931,6 +942,7 @@ struct jja_factor {
 
 struct jja_plan {
   int Nj = 0, Nf = 0, W = 0, width = 3, WB = 1, rows_per_lane = kDefaultRowsPerLane, n_levels = 0;
+  bool pdl = false;   // step kernels launched with programmatic dependent launch
   double dt = 0.0, extrap[4] = {0, 0, 0, 0};
   Tables t{};
   FactorDev F{};
@@ -981,6 +993,28 @@ struct jja_plan {
 
 namespace {
 
+// Launch with programmatic stream serialisation (the kernel overlaps its launch with the tail
+// of the previous kernel of the stream; it synchronises itself in pdl_begin), or plainly.
+template <typename... KArgs, typename... Args>
+void launch(bool pdl, void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+  if (!pdl) {
+    kernel<<<grid, block, 0, st>>>(args...);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    JJA_CUDA(cudaLaunchKernelEx(&cfg, kernel, args...));
+  }
+  g_launches++;
+}
+
 // zero the rows that partial items of the coming sweep accumulate into (and, for a dataflow
 // sweep, its counters)
 void launch_zero_rows(jja_plan* p, cudaStream_t st, bool forward, double* v) {
@@ -988,9 +1022,8 @@ void launch_zero_rows(jja_plan* p, cudaStream_t st, bool forward, double* v) {
   const int n_ctr = p->flow ? p->ns + 1 : 0;
   if (!n && !n_ctr) return;
   unsigned* ctr = p->flow ? p->counters + (forward ? 0 : p->ns + 1) : nullptr;
-  k_zero_rows<<<grid_for(std::max<int64_t>((int64_t)n * p->W, n_ctr), 256), 256, 0, st>>>(
-      v, forward ? p->zrows_f : p->zrows_b, n, p->W, ctr, n_ctr);
-  g_launches++;
+  launch(p->pdl, k_zero_rows, grid_for(std::max<int64_t>((int64_t)n * p->W, n_ctr), 256), 256, st, v,
+         (const int32_t*)(forward ? p->zrows_f : p->zrows_b), n, p->W, ctr, n_ctr);
 }
 
 template <int RPL>
@@ -1009,11 +1042,11 @@ void launch_flow(jja_plan* p, cudaStream_t st, bool forward, double* b, double* 
   if (!n) return;
   const int grid = std::max(1, std::min((n + kWarpsPerBlock - 1) / kWarpsPerBlock, p->flow_blocks[vi][forward]));
   if (forward)
-    k_flow_sweep<RPL, true><<<grid, kWarpsPerBlock * 32, 0, st>>>(p->F, p->fwd_items, n, p->W, p->WB, b, z, x, fl);
+    launch(p->pdl, k_flow_sweep<RPL, true>, grid, kWarpsPerBlock * 32, st, p->F, (const int4*)p->fwd_items, n, p->W,
+           p->WB, b, z, x, fl);
   else
-    k_flow_sweep<RPL, false><<<grid, kWarpsPerBlock * 32, 0, st>>>(p->F, p->bwd_flow_items, n, p->W, p->WB, b, z, x,
-                                                                   fl);
-  g_launches++;
+    launch(p->pdl, k_flow_sweep<RPL, false>, grid, kWarpsPerBlock * 32, st, p->F, (const int4*)p->bwd_flow_items, n,
+           p->W, p->WB, b, z, x, fl);
 }
 
 template <int RPL>
@@ -1026,17 +1059,15 @@ void launch_sweep(jja_plan* p, cudaStream_t st, bool forward, double* b, double*
     for (int l = 0; l < p->n_levels; ++l) {
       const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
       if (!n) continue;
-      k_fwd_level<RPL><<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
-          p->F, p->fwd_items + p->fwd_ptr[l], n, p->W, p->WB, b, z);
-      g_launches++;
+      launch(p->pdl, k_fwd_level<RPL>, (n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, st, p->F,
+             (const int4*)(p->fwd_items + p->fwd_ptr[l]), n, p->W, p->WB, b, z);
     }
   } else {        // levels descending; x produced
     for (int l = p->n_levels - 1; l >= 0; --l) {
       const int n = (int)(p->bwd_ptr[l + 1] - p->bwd_ptr[l]);
       if (!n) continue;
-      k_bwd_level<RPL><<<(n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, 0, st>>>(
-          p->F, p->bwd_items + p->bwd_ptr[l], n, p->W, p->WB, z, x);
-      g_launches++;
+      launch(p->pdl, k_bwd_level<RPL>, (n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, st, p->F,
+             (const int4*)(p->bwd_items + p->bwd_ptr[l]), n, p->W, p->WB, (const double*)z, x);
     }
   }
 }
@@ -1057,8 +1088,7 @@ void launch_levels(jja_plan* p, cudaStream_t st, bool forward) {
 
 // q of the first step of a run, from the phase history
 void launch_junction(jja_plan* p, StepArgs& a, cudaStream_t st) {
-  k_junction<<<grid_for((int64_t)p->Nj * p->W, 256), 256, 0, st>>>(a, p->t, p->xj);
-  g_launches++;
+  launch(p->pdl, k_junction, grid_for((int64_t)p->Nj * p->W, 256), 256, st, a, p->t, p->xj);
 }
 
 // one time step whose q is already in p->xj; `fuse_next` also leaves the next step's q there.
@@ -1066,16 +1096,14 @@ void launch_junction(jja_plan* p, StepArgs& a, cudaStream_t st) {
 void launch_step(jja_plan* p, StepArgs& a, cudaStream_t st, bool fuse_next, cudaEvent_t* ev = nullptr) {
   const int64_t NjW = (int64_t)p->Nj * p->W, NfW = (int64_t)p->Nf * p->W;
   if (ev) JJA_CUDA(cudaEventRecord(ev[0], st));
-  k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(a, p->t, p->xj, p->b);
-  g_launches++;
+  launch(p->pdl, k_face_rhs, grid_for(NfW, 256), 256, st, a, p->t, (const double*)p->xj, p->b);
   if (ev) JJA_CUDA(cudaEventRecord(ev[1], st));
   launch_levels(p, st, true);
   if (ev) JJA_CUDA(cudaEventRecord(ev[2], st));
   launch_levels(p, st, false);
   if (ev) JJA_CUDA(cudaEventRecord(ev[3], st));
-  if (fuse_next) k_update<true><<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj, p->x);
-  else k_update<false><<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj, p->x);
-  g_launches++;
+  if (fuse_next) launch(p->pdl, k_update<true>, grid_for(NjW, 256), 256, st, a, p->t, p->xj, (const double*)p->x);
+  else launch(p->pdl, k_update<false>, grid_for(NjW, 256), 256, st, a, p->t, p->xj, (const double*)p->x);
   if (ev) JJA_CUDA(cudaEventRecord(ev[4], st));
 }
 
@@ -1100,8 +1128,8 @@ StepArgs make_args(jja_plan* p, jja_state* s) {
 // refresh Is / c0 from a time-independent current-source view (before the first step of a run)
 void launch_scale_sources(jja_plan* p, jja_state* s, cudaStream_t st) {
   if (!s->Is.ptr || s->Is.stride_t) return;
-  k_scale_sources<<<grid_for((int64_t)p->Nj * p->W, 256), 256, 0, st>>>(s->Is, p->t.inv_c0, p->isq, p->Nj, p->W);
-  g_launches++;
+  launch(p->pdl, k_scale_sources, grid_for((int64_t)p->Nj * p->W, 256), 256, st, s->Is, p->t.inv_c0, p->isq, p->Nj,
+         p->W);
 }
 
 // rotate the history: the oldest buffer receives theta_next
@@ -1125,8 +1153,7 @@ void check_window(const jja_state* s, int nsteps, const char* who) {
 }
 
 void set_counters(jja_plan* p, const jja_state* s, cudaStream_t st) {
-  k_set_counters<<<1, 1, 0, st>>>(p->d_step, s->step, s->src_t0);
-  g_launches++;
+  launch(p->pdl, k_set_counters, 1, 1, st, p->d_step, s->step, s->src_t0);
 }
 
 // graph of G fused steps for the state's current buffers (captured on first use, then cached)
@@ -1273,6 +1300,7 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     const jja_solve_tuning& tu = d->tuning;
     p->WB = resolve_rhs_block(d->W, tu);
     p->rows_per_lane = tu.rows_per_lane ? tu.rows_per_lane : kDefaultRowsPerLane;
+    p->pdl = tu.pdl == 1;
     const int Nj = d->Nj, Nf = d->Nf;
     // face -> junction entries in the factor's face order; junction -> (<= 2) faces
     std::vector<int64_t> fj_ptr(Nf + 1, 0);
@@ -1344,25 +1372,17 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->t.jf_face = p->up(jf_face.data(), jf_face.size());
     p->perm = p->up(F.perm.data(), F.perm.size());
     {
-      // sin/cos of k pi/2048: first-quadrant values in extended precision, rounded once to
-      // double, then exact quadrant symmetries, so sin(m pi) and cos(m pi + pi/2) are exactly 0.
-      // Entry k: {S, C}, {-S/2, float S | float C << 32}.
-      std::vector<double2> tab(2 * (size_t)kSinTable);
+      // {sin, cos}(k pi/32768): first-quadrant values in extended precision, rounded once to
+      // double, then exact quadrant symmetries, so sin(m pi) and cos(m pi + pi/2) are exactly 0
+      std::vector<double2> tab((size_t)kSinTable);
       const long double pi_l = 3.141592653589793238462643383279502884L;
+      const int quarter = kSinTable / 4;
       for (int k = 0; k < kSinTable; ++k) {
-        const int q = k / 1024, r = k % 1024;
-        const long double ang = (long double)r * pi_l / 2048.0L;
+        const int q = k / quarter, r = k % quarter;
+        const long double ang = (long double)r * pi_l / (long double)(kSinTable / 2);
         const double s0 = (double)sinl(ang), c0 = (double)cosl(ang);
         const double sv[4] = {s0, c0, -s0, -c0}, cv[4] = {c0, -s0, -c0, s0};
-        const float sf = (float)sv[q], cf = (float)cv[q];
-        uint32_t sb, cb;
-        std::memcpy(&sb, &sf, 4);
-        std::memcpy(&cb, &cf, 4);
-        const uint64_t packed = (uint64_t)sb | ((uint64_t)cb << 32);
-        double pd;
-        std::memcpy(&pd, &packed, 8);
-        tab[2 * (size_t)k] = make_double2(sv[q], cv[q]);
-        tab[2 * (size_t)k + 1] = make_double2(-0.5 * sv[q], pd);
+        tab[(size_t)k] = make_double2(sv[q], cv[q]);
       }
       p->t.sincos = p->up(tab.data(), tab.size());
     }

@@ -66,7 +66,9 @@ def test_cache_is_written_and_reused(tmp_path, monkeypatch):
                                           ({"schedule": 2}, (-1, -1.0)),
                                           ({"schedule": 2, "rows_per_lane": 8, "rhs_block": 4}, (0, 0.0)),
                                           ({"schedule": 2, "rows_per_lane": 2, "min_piece": 4,
-                                            "target_warps": 152 * 200}, (64, 0.1))])
+                                            "target_warps": 152 * 200}, (64, 0.1)),
+                                          ({"pdl": 1}, (-1, -1.0)),
+                                          ({"pdl": 1, "schedule": 2, "rows_per_lane": 4}, (0, 0.0))])
 def test_tuned_launch_shapes_agree_with_default(tuning, relax):
     from pyjjasim_gb300 import TimeEvolutionProblem, backend
     c = SquareArray(20, 23)
