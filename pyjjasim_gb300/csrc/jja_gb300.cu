@@ -55,11 +55,20 @@ int guarded(F&& f) {
   }
 }
 
-constexpr int kWarpsPerBlock = 4;   // level kernels: one warp per work item
+#ifndef JJA_WARPS_PER_BLOCK
+#define JJA_WARPS_PER_BLOCK 4
+#endif
+// Compile-time shape of the level kernels (measured on GB300: 4 warps per block and 2 columns in
+// flight are best or tied on every workload; 8 warps per block costs 4 % at W = 512, an unroll
+// of 4 or 8 costs 6-15 % on the small-W and ragged paths, whose supernodes are narrow).
+#ifndef JJA_UNROLL
+#define JJA_UNROLL 2
+#endif
+constexpr int kWarpsPerBlock = JJA_WARPS_PER_BLOCK;   // level kernels: one warp per work item
 constexpr int kDefaultRowsPerLane = 2;   // rows of a work item handled by one lane (2, 4 or 8)
 constexpr int kDefaultTargetWarps = 152 * 24;   // levels with fewer work items split their dot products
 constexpr int kDefaultMinPiece = 16;     // shortest piece of a split dot product
-constexpr int kUnroll = 4;          // columns whose loads are issued ahead of their FMAs
+constexpr int kUnroll = JJA_UNROLL;   // columns whose loads are issued ahead of their FMAs
 constexpr double kTwoPi = 6.283185307179586;
 constexpr int kEllMax = 6;          // faces with up to 6 junctions (square 4, triangular 3, honeycomb 6)
 
