@@ -429,10 +429,18 @@ struct FactorDev {
   const double* frow;   // F_s row-major
 };
 
+// Load of a face-vector element that the item reads. In a level launch the rows an item reads
+// are final for the whole launch (this level only writes other rows: its own outputs and, by
+// atomics, its ancestors' rows), so they go through the read-only cache; in a dataflow sweep
+// other warps of the same launch may just have written them, so they are read through L2.
+template <bool kSharedLaunch>
+__device__ __forceinline__ double load_vec(const double* p) {
+  return kSharedLaunch ? __ldcg(p) : __ldg(p);
+}
+
 // One forward work item (one warp): rows [r0, r1) of F_s b_s; diagonal rows go to z, the
-// off-diagonal rows are scattered (subtracted) into the ancestors' rows of b. b is read through
-// L2 (ld.global.cg): other warps of a dataflow sweep update it with atomics while this kernel runs.
-template <int kRowsPerLane>
+// off-diagonal rows are scattered (subtracted) into the ancestors' rows of b.
+template <int kRowsPerLane, bool kSharedLaunch>
 __device__ __forceinline__ void fwd_item(const FactorDev& F, const Item& item, int lane, int W, int WB,
                                          double* __restrict__ b, double* __restrict__ z) {
   const int s = item.s, r0 = item.r0, r1 = item.r1, w0 = item.w0;
@@ -457,7 +465,7 @@ __device__ __forceinline__ void fwd_item(const FactorDev& F, const Item& item, i
   for (; j + kUnroll <= jend; j += kUnroll) {
     double bj[kUnroll], fv[kUnroll][kRowsPerLane];
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) bj[u] = __ldcg(b + (int64_t)(c0 + j + u) * W + w);
+    for (int u = 0; u < kUnroll; ++u) bj[u] = load_vec<kSharedLaunch>(b + (int64_t)(c0 + j + u) * W + w);
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u)
 #pragma unroll
@@ -468,7 +476,7 @@ __device__ __forceinline__ void fwd_item(const FactorDev& F, const Item& item, i
       for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(fv[u][t], bj[u], acc[t]);
   }
   for (; j < jend; ++j) {
-    const double bj = __ldcg(b + (int64_t)(c0 + j) * W + w);
+    const double bj = load_vec<kSharedLaunch>(b + (int64_t)(c0 + j) * W + w);
     const double* col = Fs + (int64_t)j * nf;
 #pragma unroll
     for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(__ldg(col + rr[t]), bj, acc[t]);
@@ -486,8 +494,7 @@ __device__ __forceinline__ void fwd_item(const FactorDev& F, const Item& item, i
 }
 
 // One backward work item: rows [i0, i1) of x_s = inv(L11)^T z_s - (L21 inv(L11))^T x[R_s].
-// x of the ancestors is read through L2 (written by other warps of a dataflow sweep).
-template <int kRowsPerLane>
+template <int kRowsPerLane, bool kSharedLaunch>
 __device__ __forceinline__ void bwd_item(const FactorDev& F, const Item& item, int lane, int W, int WB,
                                          const double* __restrict__ z, double* __restrict__ x) {
   const int s = item.s, i0 = item.r0, i1 = item.r1, w0 = item.w0;
@@ -542,14 +549,14 @@ __device__ __forceinline__ void bwd_item(const FactorDev& F, const Item& item, i
 #pragma unroll
       for (int t = 0; t < kRowsPerLane; ++t) fv[u][t] = __ldg(Fs + (int64_t)(k + q + u) * k + ii[t]);
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) xr[u] = __ldcg(x + (int64_t)idx[u] * W + w);
+    for (int u = 0; u < kUnroll; ++u) xr[u] = load_vec<kSharedLaunch>(x + (int64_t)idx[u] * W + w);
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u)
 #pragma unroll
       for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(-fv[u][t], xr[u], acc[t]);
   }
   for (; q < q_end; ++q) {
-    const double xr = __ldcg(x + (int64_t)__ldg(R + q) * W + w);
+    const double xr = load_vec<kSharedLaunch>(x + (int64_t)__ldg(R + q) * W + w);
     const double* row = Fs + (int64_t)(k + q) * k;
 #pragma unroll
     for (int t = 0; t < kRowsPerLane; ++t) acc[t] = fma(-__ldg(row + ii[t]), xr, acc[t]);
@@ -572,7 +579,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, 
   pdl_begin();
   const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (it >= n_items) return;
-  fwd_item<kRowsPerLane>(F, unpack_item(items[it]), threadIdx.x & 31, W, WB, b, z);
+  fwd_item<kRowsPerLane, false>(F, unpack_item(items[it]), threadIdx.x & 31, W, WB, b, z);
 }
 
 template <int kRowsPerLane>
@@ -582,7 +589,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
   pdl_begin();
   const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (it >= n_items) return;
-  bwd_item<kRowsPerLane>(F, unpack_item(items[it]), threadIdx.x & 31, W, WB, z, x);
+  bwd_item<kRowsPerLane, false>(F, unpack_item(items[it]), threadIdx.x & 31, W, WB, z, x);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -644,8 +651,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_flow_sweep(FactorDev F,
     const Item item = unpack_item(items[it]);
     if (lane == 0) flow_wait(fl, item.s);
     __syncwarp();
-    if (kForward) fwd_item<kRowsPerLane>(F, item, lane, W, WB, b, z);
-    else bwd_item<kRowsPerLane>(F, item, lane, W, WB, z, x);
+    if (kForward) fwd_item<kRowsPerLane, true>(F, item, lane, W, WB, b, z);
+    else bwd_item<kRowsPerLane, true>(F, item, lane, W, WB, z, x);
     __syncwarp();      // the warp's results, then one release fence and the completion count
     if (lane == 0) {
       const int t = __ldg(fl.notify + item.s);
