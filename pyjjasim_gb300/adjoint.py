@@ -20,7 +20,7 @@ from . import _native as N
 from .backend import GpuSimulation, _torch
 from .problem import TimeEvolutionProblem
 
-__all__ = ["AdjointRun", "time_averaged_voltage_weights", "TimeAveragedVoltageLoss"]
+__all__ = ["AdjointRun", "time_averaged_voltage_weights", "vortex_flow_weights", "TimeAveragedVoltageLoss"]
 
 
 def time_averaged_voltage_weights(problem, t1, t2, junctions=None):
@@ -32,6 +32,23 @@ def time_averaged_voltage_weights(problem, t1, t2, junctions=None):
         mask[junctions] = True
     w = np.zeros((Nj, W))
     w[mask] = 1.0 / (mask.sum() * problem._dt() * (t2 - t1))
+    return {t2: w, t1: -w}
+
+
+def vortex_flow_weights(problem, t1, t2, junctions, signs=None):
+    """Loss weights of the mean vortex flow across a line of junctions between steps t1 < t2.
+
+    A vortex crossing a junction advances its phase by 2 pi (the Josephson relation, V =
+    d theta / dt in the reference's units), so the net number of vortices crossing the line
+    per unit time is sum_j s_j (theta_j(t2) - theta_j(t1)) / (2 pi dt (t2 - t1)), with s_j = +-1
+    orienting each junction across the line (``signs``, default +1). The time-averaged vortex
+    flow is linear in the phases, as the adjoint requires; its discrete counterpart is the
+    change of the vortex configurations (TimeEvolutionResult.get_vortex_configuration)."""
+    Nj, W = problem.get_circuit()._Nj(), problem.get_problem_count()
+    junctions = np.asarray(junctions)
+    s = np.ones(len(junctions)) if signs is None else np.asarray(signs, np.float64)
+    w = np.zeros((Nj, W))
+    np.add.at(w, junctions, (s / (2 * np.pi * problem._dt() * (t2 - t1)))[:, None])
     return {t2: w, t1: -w}
 
 

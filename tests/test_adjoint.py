@@ -82,3 +82,35 @@ def test_autograd_wrapper_matches_adjoint_run():
     np.testing.assert_allclose(tIc.grad.numpy(), g["Ic"] * wts, rtol=1e-10, atol=1e-14)
     np.testing.assert_allclose(tf.grad.numpy(), g["f"] * wts, rtol=1e-10, atol=1e-14)
     np.testing.assert_allclose(tb.grad.numpy(), (g["Is"] * base[:, None]).sum(0) * wts, rtol=1e-10, atol=1e-14)
+
+
+def test_vortex_flow_gradient_matches_finite_differences():
+    """Gradient of the mean vortex flow across the middle row of horizontal junctions (a
+    linear loss of the phases) against central finite differences of the oracle."""
+    from pyjjasim_gb300.adjoint import vortex_flow_weights
+    c, Ic, f, bias, base, horiz = _setup()
+    # horizontal junctions j = y (NX - 1) + x of the middle row: the line that vortices cross
+    # when the horizontal bias drives them across the array
+    line = (NX // 2) * (NX - 1) + np.arange(NX - 1)
+    prob = _problem(c, f, bias, base)
+    run = AdjointRun(prob, vortex_flow_weights(prob, T1, T2, line), Ic=Ic)
+    g = {k: v.cpu().numpy() for k, v in run.backward().items()}
+
+    def flow(Icx, fx, bx):
+        out = []
+        for w in range(W):
+            cw = SquareArray(NX, NX)
+            cw.set_critical_current(Icx[:, w])
+            th, _, _ = rcsj_oracle.time_evolution(_problem(cw, fx[:, [w]], bx[[w]], base))
+            out.append((th[line, 0, 1] - th[line, 0, 0]).sum() / (2 * np.pi * 0.05 * (T2 - T1)))
+        return np.array(out)
+
+    np.testing.assert_allclose(run.loss.cpu().numpy(), flow(Ic, f, bias), rtol=1e-9, atol=1e-12)
+    rng = np.random.default_rng(9)
+    h = 1e-4
+    dIc, df = rng.standard_normal(Ic.shape), rng.standard_normal(f.shape)
+    for name, plus, minus, ad in (("Ic", (Ic + h * dIc, f, bias), (Ic - h * dIc, f, bias), (g["Ic"] * dIc).sum(0)),
+                                  ("f", (Ic, f + h * df, bias), (Ic, f - h * df, bias), (g["f"] * df).sum(0))):
+        fd = (flow(*plus) - flow(*minus)) / (2 * h)
+        scale = np.abs(fd).max() + 1e-12
+        assert np.abs(ad - fd).max() <= 1e-5 * scale + 1e-9, f"{name}: adjoint {ad} vs finite differences {fd}"
