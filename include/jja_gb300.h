@@ -82,7 +82,7 @@ int jja_factor_solve_host(const jja_factor* f, double* b, int nrhs);
  * project's autotuner (pyjjasim_gb300/autotune.py) times candidates and picks these. */
 typedef struct {
   int rhs_block;      /* problems per warp: a power of two <= 32 (default min(W, 32) rounded up) */
-  int rows_per_lane;  /* output rows per lane of a work item: 2, 4 or 8 (default 2) */
+  int rows_per_lane;  /* output rows per lane of a work item: 1, 2, 4 or 8 (default 1) */
   int target_warps;   /* levels with fewer work items split their dot products until they have
                          this many (default 152 x 24) */
   int min_piece;      /* shortest piece of a split dot product (default 16) */

@@ -11,7 +11,7 @@ GPU depends on choices that have no single best value across array sizes and bat
   less fill on 2-D arrays, but a deeper tree of smaller supernodes);
 * ``relax``: how far supernodes are amalgamated (fewer, wider supernodes and fewer elimination-
   tree levels, i.e. fewer launches, against extra flops on explicit zeros);
-* ``rows_per_lane`` (2, 4, 8): output rows a lane accumulates per work item (more FMAs per load
+* ``rows_per_lane`` (1, 2, 4, 8): output rows a lane accumulates per work item (more FMAs per load
   against fewer warps);
 * ``rhs_block`` (a power of two <= 32): problems a warp handles side by side (the remaining
   lanes take more rows);
@@ -34,7 +34,7 @@ import numpy as np
 from . import plan as P
 
 CACHE_ENV = "PYJJASIM_GB300_TUNE_CACHE"
-DEFAULT = {"schedule": 1, "ordering": "nd", "relax": (-1, -1.0), "rows_per_lane": 2, "rhs_block": 0,
+DEFAULT = {"schedule": 1, "ordering": "nd", "relax": (-1, -1.0), "rows_per_lane": 1, "rhs_block": 0,
            "target_warps": 152 * 24, "pdl": 0}
 # searched in this order; a tuple is searched jointly (ordering and rows per lane interact:
 # minimum degree's smaller supernodes want fewer rows per warp)
@@ -60,7 +60,7 @@ def candidates(W):
         "schedule": [1, 2],
         "pdl": [0, 1],
         "ordering": ["nd", "mmd"],
-        "rows_per_lane": [2, 4, 8],
+        "rows_per_lane": [1, 2, 4, 8],
         "rhs_block": [0] + [b for b in (wb // 2, wb // 4) if b >= 1],
         "target_warps": [152 * 24, 152 * 8, 152 * 64],
         "relax": [(-1, -1.0), (0, 0.0), (64, 0.1)],

@@ -65,7 +65,10 @@ int guarded(F&& f) {
 #define JJA_UNROLL 2
 #endif
 constexpr int kWarpsPerBlock = JJA_WARPS_PER_BLOCK;   // level kernels: one warp per work item
-constexpr int kDefaultRowsPerLane = 2;   // rows of a work item handled by one lane (2, 4 or 8)
+// rows of a work item handled by one lane (1, 2, 4 or 8). Measured on GB300: 1 and 2 tie at
+// W = 512 (1.60 ms/step), 1 is 10-12 % faster than 2 for W = 1 and ragged batches, whose
+// supernodes are narrow; 4 and 8 are slower everywhere.
+constexpr int kDefaultRowsPerLane = 1;
 constexpr int kDefaultTargetWarps = 152 * 24;   // levels with fewer work items split their dot products
 constexpr int kDefaultMinPiece = 16;     // shortest piece of a split dot product
 constexpr int kUnroll = JJA_UNROLL;   // columns whose loads are issued ahead of their FMAs
@@ -823,8 +826,9 @@ struct Schedule {
 
 Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu) {
   if (W <= 0 || W >= (1 << 30)) throw Error(JJA_ERR_ARG, "W must be in [1, 2^30)");
-  if (tu.rows_per_lane && tu.rows_per_lane != 2 && tu.rows_per_lane != 4 && tu.rows_per_lane != 8)
-    throw Error(JJA_ERR_ARG, "rows_per_lane must be 2, 4 or 8");
+  if (tu.rows_per_lane && tu.rows_per_lane != 1 && tu.rows_per_lane != 2 && tu.rows_per_lane != 4 &&
+      tu.rows_per_lane != 8)
+    throw Error(JJA_ERR_ARG, "rows_per_lane must be 1, 2, 4 or 8");
   if (tu.target_warps < 0 || tu.min_piece < 0) throw Error(JJA_ERR_ARG, "target_warps and min_piece must be >= 0");
   if (tu.schedule < 0 || tu.schedule > 2) throw Error(JJA_ERR_ARG, "schedule must be 0, 1 or 2");
   if (tu.pdl < 0 || tu.pdl > 1) throw Error(JJA_ERR_ARG, "pdl must be 0 or 1");
@@ -985,7 +989,7 @@ struct jja_plan {
   const int32_t* b_notify = nullptr;
   unsigned* counters = nullptr;   // forward: [next, done[ns]], then backward: [next, done[ns]]
   int* flow_err = nullptr;
-  int flow_blocks[3][2] = {{0, 0}, {0, 0}, {0, 0}};   // resident blocks per (rows/lane 2,4,8) x (bwd, fwd)
+  int flow_blocks[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};   // resident blocks per (rows/lane 2,4,8,1) x (bwd, fwd)
   int64_t bytes = 0;
   // captured graphs of a fixed-length step sequence, keyed by the buffers they bake in (a few
   // are kept: double-buffered source windows alternate between two keys), most recent last
@@ -1045,7 +1049,7 @@ void launch_zero_rows(jja_plan* p, cudaStream_t st, bool forward, double* v) {
 template <int RPL>
 void launch_flow(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x,
                  const uint32_t* wait_count_override = nullptr) {
-  const int vi = RPL == 2 ? 0 : (RPL == 4 ? 1 : 2);   // index into flow_blocks
+  const int vi = RPL == 2 ? 0 : (RPL == 4 ? 1 : (RPL == 8 ? 2 : 3));   // index into flow_blocks
   Flow fl;
   unsigned* base = p->counters + (forward ? 0 : p->ns + 1);
   fl.next = reinterpret_cast<int*>(base);
@@ -1091,6 +1095,7 @@ void launch_sweep(jja_plan* p, cudaStream_t st, bool forward, double* b, double*
 // one triangular sweep over the levels with the plan's rows-per-lane variant of the kernels
 void launch_sweep_any(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x) {
   switch (p->rows_per_lane) {
+    case 1: launch_sweep<1>(p, st, forward, b, z, x); break;
     case 2: launch_sweep<2>(p, st, forward, b, z, x); break;
     case 8: launch_sweep<8>(p, st, forward, b, z, x); break;
     default: launch_sweep<4>(p, st, forward, b, z, x); break;
@@ -1448,10 +1453,11 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
       int dev = 0, nsm = 0;
       JJA_CUDA(cudaGetDevice(&dev));
       JJA_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-      const void* kern[3][2] = {{(const void*)k_flow_sweep<2, false>, (const void*)k_flow_sweep<2, true>},
+      const void* kern[4][2] = {{(const void*)k_flow_sweep<2, false>, (const void*)k_flow_sweep<2, true>},
                                 {(const void*)k_flow_sweep<4, false>, (const void*)k_flow_sweep<4, true>},
-                                {(const void*)k_flow_sweep<8, false>, (const void*)k_flow_sweep<8, true>}};
-      for (int v = 0; v < 3; ++v)
+                                {(const void*)k_flow_sweep<8, false>, (const void*)k_flow_sweep<8, true>},
+                                {(const void*)k_flow_sweep<1, false>, (const void*)k_flow_sweep<1, true>}};
+      for (int v = 0; v < 4; ++v)
         for (int d = 0; d < 2; ++d) {
           int occ = 0;
           JJA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern[v][d], kWarpsPerBlock * 32, 0));
