@@ -169,6 +169,8 @@ typedef struct {
   int64_t src_t0;        /* first step held by the time-dependent views (stride_t != 0) */
   int64_t src_steps;     /* steps they hold: a call must satisfy src_t0 <= step and
                             step + nsteps <= src_t0 + src_steps */
+  int store_all;         /* 1: step i of a jja_run call is stored in slot i of th_out / I_out
+                            (th_slot / I_slot must be NULL); such runs replay CUDA graphs too */
 } jja_state;
 
 /* Runs nsteps time steps of the RCSJ update (time_evolution.py:523-580) on `stream`
@@ -210,6 +212,24 @@ typedef struct {
 } jja_adjoint_args;
 
 int jja_adjoint_step(jja_plan* p, const jja_adjoint_args* args, void* stream);
+
+/* The adjoint steps of one recomputed segment, from its last step down to its first (the loop
+ * of jja_adjoint_step calls without a host round trip per step). */
+typedef struct {
+  const double* seg;       /* device (L + 2) x Nj x W: theta_{s0-2}, theta_{s0-1}, theta_{s0}, ..., theta_{s0+L-1} */
+  int64_t s0, L, Nt;       /* first step of the segment, its length, steps of the whole run */
+  const double* const* G;  /* host array of L device pointers (Nj x W loss weights of step s0 + i) or
+                              NULL entries / NULL array where a step has none */
+  double* mu[3];           /* device (Nj x W) ring buffers of mu, indexed by step % 3 */
+  double* cos[3];          /* device (Nj x W) ring buffers of cos(phi), indexed by step % 3 */
+  double* usum;            /* accumulators as in jja_adjoint_args */
+  double* musum;
+  double* gIc;
+  int use_graph;           /* 1 (non-default stream): capture the walk once per distinct set of
+                              buffers, step % 3 phase and loss-weight pointers, then replay it */
+} jja_adjoint_segment_args;
+
+int jja_adjoint_segment(jja_plan* p, const jja_adjoint_segment_args* args, void* stream);
 /* gf (device Nf x W, original face order) = -2 pi K^{-1} A usum: the flux gradient. */
 int jja_adjoint_flux(jja_plan* p, const double* usum, double* gf, void* stream);
 

@@ -47,13 +47,20 @@ class View(ctypes.Structure):
 class State(ctypes.Structure):
     _fields_ = [("hist", c_void_p * 4), ("theta_s", c_void_p), ("Is", View), ("f", View), ("Vs", View), ("T", View),
                 ("noise_mode", c_int), ("noise", c_void_p), ("seed", ctypes.c_uint64), ("step", c_int64),
-                ("th_out", c_void_p), ("I_out", c_void_p), ("src_t0", c_int64), ("src_steps", c_int64)]
+                ("th_out", c_void_p), ("I_out", c_void_p), ("src_t0", c_int64), ("src_steps", c_int64),
+                ("store_all", c_int)]
 
 
 class AdjointArgs(ctypes.Structure):
     _fields_ = [("G", View), ("th_m1", c_void_p), ("th_m2", c_void_p), ("mu_p1", c_void_p), ("mu_p2", c_void_p),
                 ("cos_p1", c_void_p), ("cos_p2", c_void_p), ("mu_out", c_void_p), ("cos_out", c_void_p),
                 ("usum", c_void_p), ("musum", c_void_p), ("gIc", c_void_p)]
+
+
+class AdjointSegmentArgs(ctypes.Structure):
+    _fields_ = [("seg", c_void_p), ("s0", c_int64), ("L", c_int64), ("Nt", c_int64),
+                ("G", ctypes.POINTER(c_void_p)), ("mu", c_void_p * 3), ("cos", c_void_p * 3),
+                ("usum", c_void_p), ("musum", c_void_p), ("gIc", c_void_p), ("use_graph", c_int)]
 
 
 # exported symbol -> (restype, argtypes); every symbol of include/jja_gb300.h
@@ -76,6 +83,7 @@ SIGNATURES = {
     "jja_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "jja_solve_static": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "jja_adjoint_step": (c_int, [c_void_p, ctypes.POINTER(AdjointArgs), c_void_p]),
+    "jja_adjoint_segment": (c_int, [c_void_p, ctypes.POINTER(AdjointSegmentArgs), c_void_p]),
     "jja_adjoint_flux": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "jja_vortex": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "jja_eval_sin": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),

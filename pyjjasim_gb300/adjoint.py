@@ -109,26 +109,27 @@ class AdjointRun:
         mu, cs = [z() for _ in range(3)], [z() for _ in range(3)]
         usum, musum, gIc = z(), z(), z()
         h = ctypes.c_void_p(sim.stream.cuda_stream)
+        # one segment buffer for all segments: the same addresses every time, so the captured
+        # graphs of the recomputation and of the adjoint walk are replayed, not recaptured
+        S = max(s1 - s0 for s0, s1 in self.segments)
+        seg_all = torch.empty((S + 2, self.Nj, self.W), dtype=torch.float64, device=sim.dev)
         for (s0, s1), ck in reversed(list(zip(self.segments, self.checkpoints))):
             L = s1 - s0
             sim.set_history(ck, s0)
-            seg = torch.empty((L + 2, self.Nj, self.W), dtype=torch.float64, device=sim.dev)
+            seg = seg_all[:L + 2]
             seg[0].copy_(ck[1])
             seg[1].copy_(ck[0])
-            sim.run(L, np.arange(L, dtype=np.int64), None, seg[2:], None, use_graph=False)
-            for n in range(s1 - 1, s0 - 1, -1):
-                i = n - s0
-                a = N.AdjointArgs()
-                g = self.G.get(n)
-                a.G = N.View(g.data_ptr() if g is not None else None, self.W, 1)
-                a.th_m1, a.th_m2 = seg[i + 1].data_ptr(), seg[i].data_ptr()
-                if n + 1 < self.Nt:
-                    a.mu_p1, a.cos_p1 = mu[(n + 1) % 3].data_ptr(), cs[(n + 1) % 3].data_ptr()
-                if n + 2 < self.Nt:
-                    a.mu_p2, a.cos_p2 = mu[(n + 2) % 3].data_ptr(), cs[(n + 2) % 3].data_ptr()
-                a.mu_out, a.cos_out = mu[n % 3].data_ptr(), cs[n % 3].data_ptr()
-                a.usum, a.musum, a.gIc = usum.data_ptr(), musum.data_ptr(), gIc.data_ptr()
-                N.check(lib.jja_adjoint_step(sim.plan.handle, ctypes.byref(a), h))
+            sim.run(L, None, None, seg[2:], None, use_graph=True, store_all=True)
+            # the segment's adjoint steps, last to first, in one library call
+            a = N.AdjointSegmentArgs()
+            a.seg, a.s0, a.L, a.Nt = seg.data_ptr(), s0, L, self.Nt
+            gtab = (ctypes.c_void_p * L)(*[self.G[n].data_ptr() if n in self.G else None for n in range(s0, s1)])
+            a.G = ctypes.cast(gtab, ctypes.POINTER(ctypes.c_void_p))
+            for k in range(3):
+                a.mu[k], a.cos[k] = mu[k].data_ptr(), cs[k].data_ptr()
+            a.usum, a.musum, a.gIc = usum.data_ptr(), musum.data_ptr(), gIc.data_ptr()
+            a.use_graph = 1
+            N.check(lib.jja_adjoint_segment(sim.plan.handle, ctypes.byref(a), h))
         gf = torch.empty((self.Nf, self.W), dtype=torch.float64, device=sim.dev)
         N.check(lib.jja_adjoint_flux(sim.plan.handle, ctypes.c_void_p(usum.data_ptr()),
                                      ctypes.c_void_p(gf.data_ptr()), h))

@@ -272,10 +272,16 @@ class GpuSimulation:
             for s in self.windowed:
                 s.upload_window(nxt, self.window_K)
 
-    def run(self, nsteps, th_slot=None, I_slot=None, th_dev=None, I_dev=None, use_graph=True):
-        """Advance nsteps steps; step i writes th_dev[th_slot[i]] / I_dev[I_slot[i]] when >= 0."""
+    def run(self, nsteps, th_slot=None, I_slot=None, th_dev=None, I_dev=None, use_graph=True, store_all=False):
+        """Advance nsteps steps; step i writes th_dev[th_slot[i]] / I_dev[I_slot[i]] when >= 0,
+        or, with ``store_all``, th_dev[i] / I_dev[i] for every step (slots derived on the device,
+        so those runs replay CUDA graphs as well)."""
         torch, st = self.torch, self.state
         lib = N.lib()
+        if store_all and (th_slot is not None or I_slot is not None):
+            raise ValueError("store_all replaces th_slot / I_slot")
+        st.store_all = 1 if store_all else 0
+        slot_bytes = self.Nj * self.W * 8
         st.th_out = th_dev.data_ptr() if th_dev is not None else None
         st.I_out = I_dev.data_ptr() if I_dev is not None else None
         th_slot = None if th_slot is None else np.ascontiguousarray(th_slot, np.int64)
@@ -285,6 +291,9 @@ class GpuSimulation:
         while k < nsteps:
             left = self._enter_window(st.step)
             n = nsteps - k if left is None else min(nsteps - k, left)
+            if store_all:     # every call numbers its steps from 0: offset the outputs
+                st.th_out = th_dev.data_ptr() + k * slot_bytes if th_dev is not None else None
+                st.I_out = I_dev.data_ptr() + k * slot_bytes if I_dev is not None else None
             ts = None if th_slot is None else th_slot[k:k + n]
             Is_ = None if I_slot is None else I_slot[k:k + n]
             if not self.per_step_host:
@@ -293,6 +302,9 @@ class GpuSimulation:
                 self._prefetch_window()
             else:
                 for q in range(n):
+                    if store_all:
+                        st.th_out = th_dev.data_ptr() + (k + q) * slot_bytes if th_dev is not None else None
+                        st.I_out = I_dev.data_ptr() + (k + q) * slot_bytes if I_dev is not None else None
                     with torch.cuda.stream(self.stream):
                         self.noise_buf.copy_(torch.from_numpy(
                             np.array(self.noise_gen(st.step), np.float64, order="C")))

@@ -127,10 +127,11 @@ struct StepArgs {
   const double* noise;
   uint64_t seed;
   // device counters: [0] step whose face RHS comes next (written by k_update), [1] that step + 1
-  // (written by k_face_rhs), [2] first step of the time-dependent source window. Each kernel
-  // writes only a slot that no other thread of the same launch reads.
+  // (written by k_face_rhs), [2] first step of the time-dependent source window, [3] first step
+  // of the call. Each kernel writes only a slot that no other thread of the same launch reads.
   int64_t* d_step;
   int64_t th_slot, I_slot;
+  int store_all;       // every step of the call is stored, at slot (step - first step of the call)
   double* th_out;
   double* I_out;
   double e[4];
@@ -304,6 +305,7 @@ __global__ void k_set_counters(int64_t* __restrict__ d_step, int64_t step, int64
   d_step[0] = step;
   d_step[1] = step;
   d_step[2] = t0;
+  d_step[3] = step;   // first step of the call: output slot 0 when every step is stored
 }
 
 // b(p, w) = sum_j A_pj (q_j - theta_s_j) - 2 pi f_p, p in the factor's face order. Also
@@ -373,8 +375,11 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, Tables t, double* __
       for (int k = 1; k < 4; ++k) hist[k] = (k < a.width - 1) ? a.h[k - 1][e] : 0.0;
     }
     a.hout[e] = th;
-    if (a.th_out && a.th_slot >= 0) a.th_out[a.th_slot * NjW + e] = th;
-    if (a.I_out && a.I_slot >= 0) a.I_out[a.I_slot * NjW + e] = y + view_at(a.Is, j, w, tt);
+    // output slot: per step from the host, or (store_all) the step's offset in the call
+    const int64_t th_slot = a.store_all ? next_step - 1 - a.d_step[3] : a.th_slot;
+    const int64_t I_slot = a.store_all ? next_step - 1 - a.d_step[3] : a.I_slot;
+    if (a.th_out && th_slot >= 0) a.th_out[th_slot * NjW + e] = th;
+    if (a.I_out && I_slot >= 0) a.I_out[I_slot * NjW + e] = y + view_at(a.Is, j, w, tt);
     if (a.theta_s && a.Vs.ptr) a.theta_s[e] += view_at(a.Vs, j, w, tt) * a.dt;
     if (kFuseNext) q[e] = junction_q(a, t, e, j, w, hist, next_step, tt + 1);
   }
@@ -998,9 +1003,11 @@ struct jja_plan {
     cudaGraphExec_t exec;
   };
   std::vector<CachedGraph> graphs;
-  static constexpr size_t kMaxGraphs = 4;
+  std::vector<CachedGraph> adj_graphs;   // adjoint segment walks
+  static constexpr size_t kMaxGraphs = 8;
   ~jja_plan() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
+    for (auto& g : adj_graphs) cudaGraphExecDestroy(g.exec);
     for (void* p : allocs) cudaFree(p);
   }
   template <class T>
@@ -1140,6 +1147,7 @@ StepArgs make_args(jja_plan* p, jja_state* s) {
   a.d_step = p->d_step;
   a.th_out = s->th_out;
   a.I_out = s->I_out;
+  a.store_all = s->store_all ? 1 : 0;
   a.dt = p->dt;
   a.Isq = (s->Is.ptr && !s->Is.stride_t) ? jja_view{p->isq, p->W, 1, 0} : jja_view{nullptr, 0, 0, 0};
   a.resistive = p->resistive;
@@ -1181,7 +1189,9 @@ void set_counters(jja_plan* p, const jja_state* s, cudaStream_t st) {
 cudaGraphExec_t graph_for(jja_plan* p, const jja_state* s, cudaStream_t st, int G) {
   std::vector<uint64_t> key = {(uint64_t)s->hist[0], (uint64_t)s->hist[1], (uint64_t)s->hist[2],
                                (uint64_t)s->hist[3], (uint64_t)s->theta_s, (uint64_t)s->noise_mode, s->seed,
-                               (uint64_t)st, (uint64_t)G};
+                               (uint64_t)st, (uint64_t)G, (uint64_t)s->store_all,
+                               (uint64_t)(s->store_all ? s->th_out : nullptr),
+                               (uint64_t)(s->store_all ? s->I_out : nullptr)};
   for (const jja_view* v : {&s->Is, &s->f, &s->Vs, &s->T}) {
     key.push_back((uint64_t)v->ptr);
     key.push_back((uint64_t)v->stride_n);
@@ -1471,8 +1481,8 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->x = p->up<double>(nullptr, NfW);
     p->xj = p->up<double>(nullptr, NjW);
     p->isq = p->up<double>(nullptr, NjW);
-    p->d_step = p->up<int64_t>(nullptr, 3);
-    JJA_CUDA(cudaMemset(p->d_step, 0, 3 * sizeof(int64_t)));
+    p->d_step = p->up<int64_t>(nullptr, 4);
+    JJA_CUDA(cudaMemset(p->d_step, 0, 4 * sizeof(int64_t)));
     JJA_CUDA(cudaDeviceSynchronize());
     *out = p.release();
   });
@@ -1592,6 +1602,20 @@ int jja_solve_static(jja_plan* p, const double* b, double* x, void* stream) {
   });
 }
 
+// one backward-through-time step: a_n -> u = D a_n, b = A u, both sweeps, mu_n and accumulations
+static void launch_adjoint_step(jja_plan* p, const AdjArgs& a, cudaStream_t st) {
+  const int64_t NjW = (int64_t)p->Nj * p->W, NfW = (int64_t)p->Nf * p->W;
+  k_adj_a<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj);
+  StepArgs s{};
+  s.Nj = p->Nj; s.Nf = p->Nf; s.W = p->W; s.width = p->width; s.d_step = p->d_step;
+  k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(s, p->t, p->xj, p->b);
+  g_launches += 2;
+  launch_levels(p, st, true);
+  launch_levels(p, st, false);
+  k_adj_mu<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj, p->x);
+  g_launches++;
+}
+
 int jja_adjoint_step(jja_plan* p, const jja_adjoint_args* g, void* stream) {
   return guarded([&] {
     if (!p || !g) throw Error(JJA_ERR_ARG, "jja_adjoint_step: null argument");
@@ -1600,22 +1624,77 @@ int jja_adjoint_step(jja_plan* p, const jja_adjoint_args* g, void* stream) {
       throw Error(JJA_ERR_ARG, "jja_adjoint_step: missing buffer");
     if ((g->mu_p1 && !g->cos_p1) || (g->mu_p2 && !g->cos_p2))
       throw Error(JJA_ERR_ARG, "jja_adjoint_step: mu of a later step given without its cos(phi)");
-    cudaStream_t st = (cudaStream_t)stream;
     AdjArgs a{};
     a.Nj = p->Nj; a.W = p->W; a.G = g->G;
     a.th_m1 = g->th_m1; a.th_m2 = g->th_m2;
     a.mu_p1 = g->mu_p1; a.mu_p2 = g->mu_p2; a.cos_p1 = g->cos_p1; a.cos_p2 = g->cos_p2;
     a.mu_out = g->mu_out; a.cos_out = g->cos_out; a.usum = g->usum; a.musum = g->musum; a.gIc = g->gIc;
-    const int64_t NjW = (int64_t)p->Nj * p->W, NfW = (int64_t)p->Nf * p->W;
-    k_adj_a<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj);
-    StepArgs s{};
-    s.Nj = p->Nj; s.Nf = p->Nf; s.W = p->W; s.width = p->width; s.d_step = p->d_step;
-    k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(s, p->t, p->xj, p->b);
-    g_launches += 2;
-    launch_levels(p, st, true);
-    launch_levels(p, st, false);
-    k_adj_mu<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj, p->x);
-    g_launches++;
+    launch_adjoint_step(p, a, (cudaStream_t)stream);
+    JJA_CUDA(cudaGetLastError());
+  });
+}
+
+int jja_adjoint_segment(jja_plan* p, const jja_adjoint_segment_args* g, void* stream) {
+  return guarded([&] {
+    if (!p || !g || !g->seg || g->L < 0 || g->s0 < 0 || g->s0 + g->L > g->Nt)
+      throw Error(JJA_ERR_ARG, "jja_adjoint_segment: bad arguments");
+    if (p->width != 3) throw Error(JJA_ERR_ARG, "jja_adjoint_segment: the adjoint supports stencil width 3 only");
+    for (int k = 0; k < 3; ++k)
+      if (!g->mu[k] || !g->cos[k]) throw Error(JJA_ERR_ARG, "jja_adjoint_segment: missing ring buffer");
+    if (!g->usum || !g->musum || !g->gIc) throw Error(JJA_ERR_ARG, "jja_adjoint_segment: missing accumulator");
+    const int64_t NjW = (int64_t)p->Nj * p->W;
+    cudaStream_t st = (cudaStream_t)stream;
+    auto walk = [&]() {
+      for (int64_t i = g->L - 1; i >= 0; --i) {    // steps s0 + L - 1 down to s0
+        const int64_t n = g->s0 + i;
+        AdjArgs a{};
+        a.Nj = p->Nj; a.W = p->W;
+        const double* Gn = g->G ? g->G[i] : nullptr;
+        a.G = jja_view{Gn, Gn ? p->W : 0, Gn ? 1 : 0, 0};
+        a.th_m1 = g->seg + (i + 1) * NjW;          // theta_{n-1}
+        a.th_m2 = g->seg + i * NjW;                // theta_{n-2}
+        if (n + 1 < g->Nt) { a.mu_p1 = g->mu[(n + 1) % 3]; a.cos_p1 = g->cos[(n + 1) % 3]; }
+        if (n + 2 < g->Nt) { a.mu_p2 = g->mu[(n + 2) % 3]; a.cos_p2 = g->cos[(n + 2) % 3]; }
+        a.mu_out = g->mu[n % 3];
+        a.cos_out = g->cos[n % 3];
+        a.usum = g->usum; a.musum = g->musum; a.gIc = g->gIc;
+        launch_adjoint_step(p, a, st);
+      }
+    };
+    if (!g->use_graph || st == nullptr) {
+      walk();
+      JJA_CUDA(cudaGetLastError());
+      return;
+    }
+    // The launches depend on the step only through step % 3, the distance to the end of the
+    // run (missing later steps) and the loss-weight pointers: segments that agree on those and
+    // on the buffers share one captured graph.
+    std::vector<uint64_t> key = {(uint64_t)g->seg, (uint64_t)g->L, (uint64_t)(g->s0 % 3),
+                                 (uint64_t)std::min<int64_t>(g->Nt - g->s0 - g->L, 3), (uint64_t)st,
+                                 (uint64_t)g->usum, (uint64_t)g->musum, (uint64_t)g->gIc};
+    for (int k = 0; k < 3; ++k) {
+      key.push_back((uint64_t)g->mu[k]);
+      key.push_back((uint64_t)g->cos[k]);
+    }
+    for (int64_t i = 0; i < g->L; ++i) key.push_back((uint64_t)(g->G ? g->G[i] : nullptr));
+    cudaGraphExec_t exec = nullptr;
+    for (size_t k = 0; k < p->adj_graphs.size(); ++k)
+      if (p->adj_graphs[k].key == key) { exec = p->adj_graphs[k].exec; break; }
+    if (!exec) {
+      if (p->adj_graphs.size() >= jja_plan::kMaxGraphs) {
+        cudaGraphExecDestroy(p->adj_graphs.front().exec);
+        p->adj_graphs.erase(p->adj_graphs.begin());
+      }
+      cudaGraph_t graph;
+      JJA_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      walk();
+      JJA_CUDA(cudaStreamEndCapture(st, &graph));
+      const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) throw Error(JJA_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+      p->adj_graphs.push_back({key, exec});
+    }
+    JJA_CUDA(cudaGraphLaunch(exec, st));
     JJA_CUDA(cudaGetLastError());
   });
 }
@@ -1666,6 +1745,8 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
     for (int k = 0; k < p->width - 1; ++k)
       if (!s->hist[k]) throw Error(JJA_ERR_ARG, "jja_run: missing history buffer");
     if (s->noise_mode == JJA_NOISE_BUFFER && !s->noise) throw Error(JJA_ERR_ARG, "jja_run: noise buffer missing");
+    if (s->store_all && (th_slot || I_slot))
+      throw Error(JJA_ERR_ARG, "jja_run: store_all replaces th_slot / I_slot (pass NULL)");
     if (nsteps == 0) return;
     check_window(s, nsteps, "jja_run");
     cudaStream_t st = (cudaStream_t)stream;
@@ -1679,9 +1760,10 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
     const int G = 16 * period;        // steps per captured graph: pointers return to their places
     int i = 0;
     while (i < nsteps) {
-      // a run of steps that store nothing can be replayed from a captured graph; the call's
-      // last step stays out of it (it runs unfused: the look-ahead q it would evaluate belongs
-      // to a step outside this call, whose sources may lie outside the source window)
+      // a run of steps that store nothing (or, with store_all, whose slots the device derives
+      // from the step counter) can be replayed from a captured graph; the call's last step
+      // stays out of it (it runs unfused: the look-ahead q it would evaluate belongs to a step
+      // outside this call, whose sources may lie outside the source window)
       int run = 0;
       while (i + run < nsteps && (!th_slot || th_slot[i + run] < 0) && (!I_slot || I_slot[i + run] < 0)) ++run;
       const int graphable = (i + run == nsteps) ? run - 1 : run;

@@ -120,6 +120,30 @@ def test_graph_and_eager_paths_agree():
     close(th_g, th_e, rtol=1e-11)
 
 
+def test_store_all_matches_per_step_slots():
+    """Storing every step with slots derived on the device (graph replays) gives the same
+    phases and currents as per-step slots from the host (eager launches)."""
+    import torch
+    c = SquareArray(17, 13)
+    W, L = 5, 150
+    Is = c.current_base(0.0)[:, None, None] * np.linspace(0.5, 1.5, W)[None, :, None]
+    prob = TimeEvolutionProblem(c, time_step=0.05, time_step_count=L, current_sources=Is, external_flux=0.2)
+    out = []
+    for store_all in (False, True):
+        sim = backend.GpuSimulation(prob)
+        th = torch.empty((L, c.junction_count(), W), dtype=torch.float64, device=sim.dev)
+        I = torch.empty_like(th)
+        with torch.cuda.stream(sim.stream):
+            if store_all:
+                sim.run(L, None, None, th, I, use_graph=True, store_all=True)
+            else:
+                sim.run(L, np.arange(L), np.arange(L), th, I, use_graph=False)
+        sim.synchronize()
+        out.append((th.cpu().numpy(), I.cpu().numpy()))
+    close(out[1][0], out[0][0], rtol=1e-12)
+    close(out[1][1], out[0][1], rtol=1e-12)
+
+
 def test_full_size_kirchhoff_invariants():
     """IV-sweep shape at full size (128x128 array, W=512): A theta + 2 pi f = 0 (no inductance)
     and current conservation M (I - Is) = 0 after many steps; both are size-independent."""
