@@ -89,6 +89,8 @@ typedef struct {
   int schedule;       /* 1: one launch per elimination-tree level; 2: dataflow, one persistent
                          launch per sweep whose work items wait (bounded) on per-supernode
                          completion counters; 0: default (1) */
+  int rows_per_lane_fwd; /* rows per lane of the forward sweep alone (0: rows_per_lane if set,
+                            else the forward default: 2 for W >= 256, 1 below) */
   int pdl;            /* 1: launch the step's kernels with programmatic dependent launch (each
                          launch overlaps the tail of the kernel before; measured: 6 % faster for
                          W = 1, 5-7 % slower for W >= 64); 0: default (plain launches) */

@@ -34,11 +34,13 @@ import numpy as np
 from . import plan as P
 
 CACHE_ENV = "PYJJASIM_GB300_TUNE_CACHE"
-DEFAULT = {"schedule": 1, "ordering": "nd", "relax": (-1, -1.0), "rows_per_lane": 1, "rhs_block": 0,
-           "target_warps": 152 * 24, "pdl": 0}
+DEFAULT = {"schedule": 1, "ordering": "nd", "relax": (-1, -1.0), "rows_per_lane": 0, "rows_per_lane_fwd": 0,
+           "rhs_block": 0, "target_warps": 152 * 24, "pdl": 0}
 # searched in this order; a tuple is searched jointly (ordering and rows per lane interact:
-# minimum degree's smaller supernodes want fewer rows per warp)
-AXES = (("ordering", "rows_per_lane"), "schedule", "pdl", "rhs_block", "target_warps", "relax")
+# minimum degree's smaller supernodes want fewer rows per warp). Rows per lane 0 = the library's
+# defaults (1, and 2 in the forward sweep from W = 256 on); a nonzero value sets both sweeps
+# unless rows_per_lane_fwd sets the forward one.
+AXES = (("ordering", "rows_per_lane"), "rows_per_lane_fwd", "schedule", "pdl", "rhs_block", "target_warps", "relax")
 
 
 def cache_path():
@@ -60,7 +62,8 @@ def candidates(W):
         "schedule": [1, 2],
         "pdl": [0, 1],
         "ordering": ["nd", "mmd"],
-        "rows_per_lane": [1, 2, 4, 8],
+        "rows_per_lane": [0, 1, 2, 4],
+        "rows_per_lane_fwd": [0, 1, 2, 4],
         "rhs_block": [0] + [b for b in (wb // 2, wb // 4) if b >= 1],
         "target_warps": [152 * 24, 152 * 8, 152 * 64],
         "relax": [(-1, -1.0), (0, 0.0), (64, 0.1)],
@@ -70,9 +73,10 @@ def candidates(W):
 def to_options(cfg):
     """GpuSimulation options of a configuration."""
     return {"ordering": str(cfg["ordering"]), "relax": tuple(cfg["relax"]),
-            "tuning": {"rows_per_lane": int(cfg["rows_per_lane"]), "rhs_block": int(cfg["rhs_block"]),
-                       "target_warps": int(cfg["target_warps"]), "schedule": int(cfg["schedule"]),
-                       "pdl": int(cfg.get("pdl", 0))}}
+            "tuning": {"rows_per_lane": int(cfg["rows_per_lane"]),
+                       "rows_per_lane_fwd": int(cfg.get("rows_per_lane_fwd", 0)),
+                       "rhs_block": int(cfg["rhs_block"]), "target_warps": int(cfg["target_warps"]),
+                       "schedule": int(cfg["schedule"]), "pdl": int(cfg.get("pdl", 0))}}
 
 
 def coordinate_descent(W, measure, min_gain=0.02):

@@ -69,6 +69,7 @@ constexpr int kWarpsPerBlock = JJA_WARPS_PER_BLOCK;   // level kernels: one warp
 // W = 512 (1.60 ms/step), 1 is 10-12 % faster than 2 for W = 1 and ragged batches, whose
 // supernodes are narrow; 4 and 8 are slower everywhere.
 constexpr int kDefaultRowsPerLane = 1;
+constexpr int kDefaultRowsPerLaneFwdWide = 2;   // the forward sweep's default for W >= 256
 constexpr int kDefaultTargetWarps = 152 * 24;   // levels with fewer work items split their dot products
 constexpr int kDefaultMinPiece = 16;     // shortest piece of a split dot product
 constexpr int kUnroll = JJA_UNROLL;   // columns whose loads are issued ahead of their FMAs
@@ -802,6 +803,17 @@ T* upload(const T* h, size_t n, int64_t& bytes) {
   return d;
 }
 
+// rows per lane of the forward or backward sweep: rows_per_lane_fwd (forward only) overrides
+// rows_per_lane, which sets both; unset fields take each sweep's default. Measured on GB300
+// (ms/step, forward/backward rows): W = 512: 1/1 1.554, 2/1 1.511, 2/2 1.579; W = 1: 1/1 0.133,
+// 2/1 0.138; 64x64 x 64: 1/1 0.138, 2/1 0.141; so two forward rows from W = 256 on.
+int rows_per_lane_of(const jja_solve_tuning& tu, bool forward, int W) {
+  if (forward && tu.rows_per_lane_fwd) return tu.rows_per_lane_fwd;
+  if (tu.rows_per_lane) return tu.rows_per_lane;
+  if (forward) return W >= 256 ? kDefaultRowsPerLaneFwdWide : kDefaultRowsPerLane;
+  return kDefaultRowsPerLane;
+}
+
 // problems per warp of the triangular solves
 int resolve_rhs_block(int W, const jja_solve_tuning& tu) {
   int WB = 1;
@@ -831,17 +843,17 @@ struct Schedule {
 
 Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu) {
   if (W <= 0 || W >= (1 << 30)) throw Error(JJA_ERR_ARG, "W must be in [1, 2^30)");
-  if (tu.rows_per_lane && tu.rows_per_lane != 1 && tu.rows_per_lane != 2 && tu.rows_per_lane != 4 &&
-      tu.rows_per_lane != 8)
-    throw Error(JJA_ERR_ARG, "rows_per_lane must be 1, 2, 4 or 8");
+  for (int v : {tu.rows_per_lane, tu.rows_per_lane_fwd})
+    if (v && v != 1 && v != 2 && v != 4 && v != 8)
+      throw Error(JJA_ERR_ARG, "rows_per_lane and rows_per_lane_fwd must be 1, 2, 4 or 8");
   if (tu.target_warps < 0 || tu.min_piece < 0) throw Error(JJA_ERR_ARG, "target_warps and min_piece must be >= 0");
   if (tu.schedule < 0 || tu.schedule > 2) throw Error(JJA_ERR_ARG, "schedule must be 0, 1 or 2");
   if (tu.pdl < 0 || tu.pdl > 1) throw Error(JJA_ERR_ARG, "pdl must be 0 or 1");
   const int WB = resolve_rhs_block(W, tu);
-  const int rpl = tu.rows_per_lane ? tu.rows_per_lane : kDefaultRowsPerLane;
   const int target_warps = tu.target_warps ? tu.target_warps : kDefaultTargetWarps;
   const int min_piece = tu.min_piece ? tu.min_piece : kDefaultMinPiece;
-  const int LG = 32 / WB, RPI = LG * rpl;
+  const int LG = 32 / WB;
+  const int RPI_f = LG * rows_per_lane_of(tu, true, W), RPI_b = LG * rows_per_lane_of(tu, false, W);
   Schedule S;
   S.n_levels = F.n_levels;
   S.ns = F.ns;
@@ -868,8 +880,8 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu)
     int64_t nfw = 0, nbw = 0;
     for (int s : by_level[l]) {
       const int k = F.sn_k[s], nf = k + F.sn_m[s];
-      nfw += (int64_t)((nf + RPI - 1) / RPI) * nwc;
-      nbw += (int64_t)((k + RPI - 1) / RPI) * nwc;
+      nfw += (int64_t)((nf + RPI_f - 1) / RPI_f) * nwc;
+      nbw += (int64_t)((k + RPI_b - 1) / RPI_b) * nwc;
     }
     const int fsplit = (int)std::max<int64_t>(1, (target_warps + nfw - 1) / std::max<int64_t>(nfw, 1));
     const int bsplit = (int)std::max<int64_t>(1, (target_warps + nbw - 1) / std::max<int64_t>(nbw, 1));
@@ -877,16 +889,16 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu)
       const int k = F.sn_k[s], nf = k + F.sn_m[s], c0 = F.sn_col0[s];
       bool zf_s = false, zb_s = false;
       const int fplen = pieces_of(k, fsplit);
-      for (int r0 = 0; r0 < nf; r0 += RPI) {
-        const int r1 = std::min(nf, r0 + RPI), jmax = std::min(k, r1);
+      for (int r0 = 0; r0 < nf; r0 += RPI_f) {
+        const int r1 = std::min(nf, r0 + RPI_f), jmax = std::min(k, r1);
         const bool partial = jmax > fplen;
         zf_s |= partial && r0 < k;
         for (int c_lo = 0; c_lo < jmax; c_lo += fplen)
           for (int w0 = 0; w0 < W; w0 += WB)
             S.fi.push_back(pack(s, r0, r1, w0, partial, c_lo, std::min(jmax, c_lo + fplen)));
       }
-      for (int i0 = 0; i0 < k; i0 += RPI) {
-        const int i1 = std::min(k, i0 + RPI), len = nf - i0;
+      for (int i0 = 0; i0 < k; i0 += RPI_b) {
+        const int i1 = std::min(k, i0 + RPI_b), len = nf - i0;
         const int bplen = pieces_of(len, bsplit);
         const bool partial = len > bplen;
         zb_s |= partial;
@@ -966,7 +978,8 @@ struct jja_factor {
 };
 
 struct jja_plan {
-  int Nj = 0, Nf = 0, W = 0, width = 3, WB = 1, rows_per_lane = kDefaultRowsPerLane, n_levels = 0;
+  int Nj = 0, Nf = 0, W = 0, width = 3, WB = 1, n_levels = 0;
+  int rows_per_lane = kDefaultRowsPerLane, rows_per_lane_fwd = kDefaultRowsPerLane;   // backward, forward
   bool pdl = false;   // step kernels launched with programmatic dependent launch
   double dt = 0.0, extrap[4] = {0, 0, 0, 0};
   Tables t{};
@@ -1101,7 +1114,7 @@ void launch_sweep(jja_plan* p, cudaStream_t st, bool forward, double* b, double*
 
 // one triangular sweep over the levels with the plan's rows-per-lane variant of the kernels
 void launch_sweep_any(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x) {
-  switch (p->rows_per_lane) {
+  switch (forward ? p->rows_per_lane_fwd : p->rows_per_lane) {
     case 1: launch_sweep<1>(p, st, forward, b, z, x); break;
     case 2: launch_sweep<2>(p, st, forward, b, z, x); break;
     case 8: launch_sweep<8>(p, st, forward, b, z, x); break;
@@ -1330,7 +1343,8 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     // by build_schedule
     const jja_solve_tuning& tu = d->tuning;
     p->WB = resolve_rhs_block(d->W, tu);
-    p->rows_per_lane = tu.rows_per_lane ? tu.rows_per_lane : kDefaultRowsPerLane;
+    p->rows_per_lane = rows_per_lane_of(tu, false, d->W);
+    p->rows_per_lane_fwd = rows_per_lane_of(tu, true, d->W);
     p->pdl = tu.pdl == 1;
     const int Nj = d->Nj, Nf = d->Nf;
     // face -> junction entries in the factor's face order; junction -> (<= 2) faces

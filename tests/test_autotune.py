@@ -10,17 +10,17 @@ from pyjjasim_gb300.circuit import SquareArray
 
 
 def test_coordinate_descent_finds_the_fastest_axis_values():
-    # synthetic cost: rows_per_lane 8 and target_warps 152*8 help, relax (0, 0) hurts
+    # synthetic cost: rows_per_lane 4 and target_warps 152*8 help, relax (0, 0) hurts
     def measure(cfg):
         t = 1.0
-        t *= 0.8 if cfg["rows_per_lane"] == 8 else 1.0
+        t *= 0.8 if cfg["rows_per_lane"] == 4 else 1.0
         t *= 0.9 if cfg["target_warps"] == 152 * 8 else 1.0
         t *= 1.3 if tuple(cfg["relax"]) == (0, 0.0) else 1.0
         t *= 0.99 if cfg["rhs_block"] == 16 else 1.0     # below the 2 % threshold: not taken
         return t
 
     best, t, log = AT.coordinate_descent(512, measure)
-    assert best["rows_per_lane"] == 8 and best["target_warps"] == 152 * 8
+    assert best["rows_per_lane"] == 4 and best["target_warps"] == 152 * 8
     assert tuple(best["relax"]) == (-1, -1.0) and best["rhs_block"] == 0
     assert best["schedule"] == 1 and best["ordering"] == "nd"
     assert t == pytest.approx(0.72)

@@ -115,3 +115,29 @@ def test_dataflow_schedule_waits_only_on_earlier_items(make, ordering, W, tuning
     f = P.HostFactor(K, coords=coords, perm=perm)
     nf, nb = f.check_schedule(W, tuning)
     assert nf >= f.stats["n_supernodes"] and nb >= f.stats["n_supernodes"]
+
+
+def test_ctypes_structs_match_the_header():
+    """Field names and order of the ctypes mirrors equal the C structs in include/jja_gb300.h."""
+    text = open(os.path.join(os.path.dirname(__file__), "..", "include", "jja_gb300.h")).read()
+
+    def c_fields(name):
+        end = text.index("} " + name + ";")
+        start = text.rindex("typedef struct {", 0, end)
+        body = re.sub(r"/\*.*?\*/", "", text[start:end], flags=re.S)
+        out = []
+        for decl in body.split(";")[:-1]:
+            decl = decl.replace("typedef struct {", "").strip()
+            if not decl:
+                continue
+            names = decl.split(",")
+            first = re.findall(r"(\w+)\s*(?:\[\d+\])?$", names[0].strip())[0]
+            out.append(first)
+            out.extend(re.findall(r"\**\s*(\w+)", n)[0] for n in names[1:])
+        return out
+
+    for cname, pystruct in (("jja_solve_tuning", N.SolveTuning), ("jja_view", N.View), ("jja_state", N.State),
+                            ("jja_plan_desc", N.PlanDesc), ("jja_adjoint_args", N.AdjointArgs),
+                            ("jja_adjoint_segment_args", N.AdjointSegmentArgs), ("jja_factor_opts", N.FactorOpts),
+                            ("jja_factor_stats", N.FactorStats)):
+        assert c_fields(cname) == [f for f, _ in pystruct._fields_], cname
