@@ -91,6 +91,11 @@ typedef struct {
                          completion counters; 0: default (1) */
   int rows_per_lane_fwd; /* rows per lane of the forward sweep alone (0: rows_per_lane if set,
                             else the forward default: 2 for W >= 256, 1 below) */
+  int pack_rows;      /* W = 1, level schedule: supernodes of at most this many rows (and at most 8
+                         columns) are solved one per lane, 32 per warp (0: default 24; negative:
+                         never) ... */
+  int pack_min_warps; /* ... on levels whose regular items need at least this many warps
+                         (0: default 19456, two waves of 152 SMs x 64 warps) */
   int pdl;            /* 1: launch the step's kernels with programmatic dependent launch (each
                          launch overlaps the tail of the kernel before; measured: 6 % faster for
                          W = 1, 5-7 % slower for W >= 64); 0: default (plain launches) */

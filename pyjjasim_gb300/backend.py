@@ -410,8 +410,9 @@ def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", se
     return th_buf.transpose(1, 2, 0), I_buf.transpose(1, 2, 0)
 
 
-def solve_faces(circuit, dt, b, stencil_width=3, nd_leaf=8):
-    """K^{-1} b on the GPU for (Nf, W) right-hand sides (the per-step face-space solve)."""
+def solve_faces(circuit, dt, b, stencil_width=3, nd_leaf=8, ordering="nd", tuning=None):
+    """K^{-1} b on the GPU for (Nf, W) right-hand sides (the per-step face-space solve);
+    ``ordering`` and ``tuning`` as for the simulation's plan."""
     from .problem import stencil
     torch = _torch()
     b = np.ascontiguousarray(b, np.float64)
@@ -419,7 +420,8 @@ def solve_faces(circuit, dt, b, stencil_width=3, nd_leaf=8):
     if squeeze:
         b = b[:, None]
     W = b.shape[1]
-    pl = P.get_plan(circuit, dt, W, stencil_width, stencil(stencil_width), nd_leaf=nd_leaf)
+    pl = P.get_plan(circuit, dt, W, stencil_width, stencil(stencil_width), nd_leaf=nd_leaf, ordering=ordering,
+                    tuning=tuning)
     st = torch.cuda.Stream()
     with torch.cuda.stream(st):
         bd = torch.from_numpy(b).cuda()

@@ -70,6 +70,9 @@ constexpr int kWarpsPerBlock = JJA_WARPS_PER_BLOCK;   // level kernels: one warp
 // supernodes are narrow; 4 and 8 are slower everywhere.
 constexpr int kDefaultRowsPerLane = 1;
 constexpr int kDefaultRowsPerLaneFwdWide = 2;   // the forward sweep's default for W >= 256
+constexpr int kDefaultPackRows = 24;   // W = 1: supernodes of at most this many rows go one per lane
+constexpr int kPackMaxK = 8;           // ... and at most this many columns
+constexpr int kDefaultPackMinWarps = 152 * 64 * 2;   // ... on levels with at least two waves of warps
 constexpr int kDefaultTargetWarps = 152 * 24;   // levels with fewer work items split their dot products
 constexpr int kDefaultMinPiece = 16;     // shortest piece of a split dot product
 constexpr int kUnroll = JJA_UNROLL;   // columns whose loads are issued ahead of their FMAs
@@ -427,6 +430,15 @@ __global__ void k_zero_rows(double* __restrict__ v, const int32_t* __restrict__ 
   for (int64_t e = tid; e < n_ctr; e += nth) ctr[e] = 0u;
 }
 
+// Load of a face-vector element that the item reads. In a level launch the rows an item reads
+// are final for the whole launch (this level only writes other rows: its own outputs and, by
+// atomics, its ancestors' rows), so they go through the read-only cache; in a dataflow sweep
+// other warps of the same launch may just have written them, so they are read through L2.
+template <bool kSharedLaunch>
+__device__ __forceinline__ double load_vec(const double* p) {
+  return kSharedLaunch ? __ldcg(p) : __ldg(p);
+}
+
 struct FactorDev {
   const int32_t* col0;
   const int32_t* k;
@@ -436,15 +448,84 @@ struct FactorDev {
   const int64_t* valptr;
   const double* fcol;   // F_s column-major ((k+m) x k)
   const double* frow;   // F_s row-major
+  const int4* pack_meta;     // W = 1 packs: per lane (col0, k, k + m, rowptr) of its supernode
+  const double* pack_vals;   // W = 1 packs: the F_s of a pack's supernodes interleaved by lane
 };
 
-// Load of a face-vector element that the item reads. In a level launch the rows an item reads
-// are final for the whole launch (this level only writes other rows: its own outputs and, by
-// atomics, its ancestors' rows), so they go through the read-only cache; in a dataflow sweep
-// other warps of the same launch may just have written them, so they are read through L2.
-template <bool kSharedLaunch>
-__device__ __forceinline__ double load_vec(const double* p) {
-  return kSharedLaunch ? __ldcg(p) : __ldg(p);
+// W = 1 packs. A work item whose x field is negative covers up to 32 small supernodes of one
+// level, one per lane: pack p = -1 - x, y lanes, z = NP | KP << 16 (the largest row and column
+// count among them), w = offset of its values in units of 32 doubles. F_s(r, j) of lane l sits at
+// pack_vals[32 (w + j NP + r) + l], zero padded to NP x KP, so every load instruction of the warp
+// reads 256 contiguous bytes while each lane walks its own supernode. Levels with many more
+// small supernodes than a wave of warps use them: a regular item there leaves most lanes idle and
+// pays a chain of dependent loads for a handful of FMAs. KM (>= KP) sizes the register arrays.
+template <int KM>
+__device__ __forceinline__ void fwd_pack(const FactorDev& F, const int4 raw, int lane, double* __restrict__ b,
+                                         double* __restrict__ z) {
+  if (lane >= raw.y) return;
+  const int NP = raw.z & 0xffff, KP = raw.z >> 16;
+  const int4 meta = __ldg(F.pack_meta + (int64_t)(-1 - raw.x) * 32 + lane);
+  const int c0 = meta.x, k = meta.y, nf = meta.z;
+  const int32_t* R = F.rows + meta.w;
+  // the supernode's own rows of b are final (its descendants sit on earlier levels) and no item
+  // of this level writes them
+  double bv[KM];
+#pragma unroll
+  for (int j = 0; j < KM; ++j) bv[j] = j < k ? __ldg(b + c0 + j) : 0.0;
+  const double* V = F.pack_vals + (int64_t)raw.w * 32 + lane;
+  // rows unrolled so that about 16 loads of each lane are in flight
+#pragma unroll(16 / KM)
+  for (int r = 0; r < NP; ++r) {
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < KM; ++j)
+      if (j < KP) acc = fma(__ldg(V + ((int64_t)j * NP + r) * 32), bv[j], acc);
+    if (r < k) z[c0 + r] = acc;
+    else if (r < nf) atomicAdd(b + __ldg(R + (r - k)), -acc);
+  }
+}
+
+template <int KM>
+__device__ __forceinline__ void bwd_pack(const FactorDev& F, const int4 raw, int lane, const double* __restrict__ z,
+                                         double* __restrict__ x) {
+  if (lane >= raw.y) return;
+  const int NP = raw.z & 0xffff, KP = raw.z >> 16;
+  const int4 meta = __ldg(F.pack_meta + (int64_t)(-1 - raw.x) * 32 + lane);
+  const int c0 = meta.x, k = meta.y, nf = meta.z;
+  const int32_t* R = F.rows + meta.w;
+  const double* V = F.pack_vals + (int64_t)raw.w * 32 + lane;
+  double acc[KM];
+#pragma unroll
+  for (int i = 0; i < KM; ++i) acc[i] = 0.0;
+  // x_s = F11^T z_s - F21^T x_R: the ancestors' rows of x were written by earlier launches
+#pragma unroll(16 / KM)
+  for (int r = 0; r < NP; ++r) {
+    double v = 0.0;
+    if (r < k) v = __ldg(z + c0 + r);
+    else if (r < nf) v = -__ldg(x + __ldg(R + (r - k)));
+#pragma unroll
+    for (int i = 0; i < KM; ++i)
+      if (i < KP) acc[i] = fma(__ldg(V + ((int64_t)i * NP + r) * 32), v, acc[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < KM; ++i)
+    if (i < k) x[c0 + i] = acc[i];
+}
+
+__device__ __forceinline__ void fwd_pack_any(const FactorDev& F, const int4 raw, int lane, double* __restrict__ b,
+                                             double* __restrict__ z) {
+  const int KP = raw.z >> 16;
+  if (KP <= 2) fwd_pack<2>(F, raw, lane, b, z);
+  else if (KP <= 4) fwd_pack<4>(F, raw, lane, b, z);
+  else fwd_pack<kPackMaxK>(F, raw, lane, b, z);
+}
+
+__device__ __forceinline__ void bwd_pack_any(const FactorDev& F, const int4 raw, int lane,
+                                             const double* __restrict__ z, double* __restrict__ x) {
+  const int KP = raw.z >> 16;
+  if (KP <= 2) bwd_pack<2>(F, raw, lane, z, x);
+  else if (KP <= 4) bwd_pack<4>(F, raw, lane, z, x);
+  else bwd_pack<kPackMaxK>(F, raw, lane, z, x);
 }
 
 // One forward work item (one warp): rows [r0, r1) of F_s b_s; diagonal rows go to z, the
@@ -580,25 +661,31 @@ __device__ __forceinline__ void bwd_item(const FactorDev& F, const Item& item, i
   (void)m;
 }
 
-// level-synchronous sweeps: one launch per elimination-tree level, one warp per item
-template <int kRowsPerLane>
+// level-synchronous sweeps: one launch per elimination-tree level, one warp per item (kPacks:
+// the level also holds W = 1 packs; a separate instantiation keeps their registers out of the
+// regular kernels)
+template <int kRowsPerLane, bool kPacks>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, const int4* __restrict__ items,
                                                                    int n_items, int W, int WB,
                                                                    double* __restrict__ b, double* __restrict__ z) {
   pdl_begin();
   const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (it >= n_items) return;
-  fwd_item<kRowsPerLane, false>(F, unpack_item(items[it]), threadIdx.x & 31, W, WB, b, z);
+  const int4 raw = items[it];
+  if (kPacks && raw.x < 0) fwd_pack_any(F, raw, threadIdx.x & 31, b, z);
+  else fwd_item<kRowsPerLane, false>(F, unpack_item(raw), threadIdx.x & 31, W, WB, b, z);
 }
 
-template <int kRowsPerLane>
+template <int kRowsPerLane, bool kPacks>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, const int4* __restrict__ items,
                                                                    int n_items, int W, int WB,
                                                                    const double* __restrict__ z, double* __restrict__ x) {
   pdl_begin();
   const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (it >= n_items) return;
-  bwd_item<kRowsPerLane, false>(F, unpack_item(items[it]), threadIdx.x & 31, W, WB, z, x);
+  const int4 raw = items[it];
+  if (kPacks && raw.x < 0) bwd_pack_any(F, raw, threadIdx.x & 31, z, x);
+  else bwd_item<kRowsPerLane, false>(F, unpack_item(raw), threadIdx.x & 31, W, WB, z, x);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -833,13 +920,31 @@ struct Schedule {
   std::vector<int4> bi;        // backward items, levels ascending (level launches run them per level, root first)
   std::vector<int4> bi_flow;   // the backward items root first (the dataflow sweep takes them in this order)
   std::vector<int64_t> fwd_ptr, bwd_ptr;   // per level, into fi / bi
+  std::vector<char> level_packed;          // per level: holds W = 1 packs
   std::vector<int32_t> zf, zb;             // rows of z / x that partial items accumulate into
   // forward: items of s wait until done[fon[s]] == fcnt[s] (fon[s] = s or -1) and then count
   // towards fnot[s] (the parent); backward: items of s wait until done[bon[s]] == bcnt[s]
   // (bon[s] = parent or -1) and count towards bnot[s] (s itself, if it has children)
   std::vector<int32_t> fon, fnot, bon, bnot;
   std::vector<uint32_t> fcnt, bcnt;
+  // W = 1 packs (level schedule only): 32 lanes each, the supernode of every lane (-1: none),
+  // its (col0, k, k + m, rowptr) and the interleaved values (see fwd_pack)
+  std::vector<int32_t> pack_sn;
+  std::vector<int4> pack_meta;
+  std::vector<double> pack_vals;
 };
+
+// the supernodes a work item covers: one, or the members of a W = 1 pack
+template <class Fn>
+void for_each_supernode(const Schedule& S, const int4& v, Fn fn) {
+  if (v.x >= 0) {
+    fn(v.x);
+    return;
+  }
+  const int64_t first = (-1 - (int64_t)v.x) * 32;
+  if (v.y < 1 || v.y > 32 || first + 32 > (int64_t)S.pack_sn.size()) throw Error(JJA_ERR_INTERNAL, "pack out of range");
+  for (int l = 0; l < v.y; ++l) fn(S.pack_sn[first + l]);
+}
 
 Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu) {
   if (W <= 0 || W >= (1 << 30)) throw Error(JJA_ERR_ARG, "W must be in [1, 2^30)");
@@ -849,7 +954,14 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu)
   if (tu.target_warps < 0 || tu.min_piece < 0) throw Error(JJA_ERR_ARG, "target_warps and min_piece must be >= 0");
   if (tu.schedule < 0 || tu.schedule > 2) throw Error(JJA_ERR_ARG, "schedule must be 0, 1 or 2");
   if (tu.pdl < 0 || tu.pdl > 1) throw Error(JJA_ERR_ARG, "pdl must be 0 or 1");
+  if (tu.pack_rows > 256) throw Error(JJA_ERR_ARG, "pack_rows must be <= 256");
+  if (tu.pack_min_warps < 0) throw Error(JJA_ERR_ARG, "pack_min_warps must be >= 0");
   const int WB = resolve_rhs_block(W, tu);
+  // W = 1 packs of small supernodes (level schedule only: the dataflow sweep counts items per
+  // supernode)
+  const int pack_rows = (W == 1 && tu.schedule != 2 && tu.pack_rows >= 0)
+                            ? (tu.pack_rows ? tu.pack_rows : kDefaultPackRows) : 0;
+  const int64_t pack_min_warps = tu.pack_min_warps ? tu.pack_min_warps : kDefaultPackMinWarps;
   const int target_warps = tu.target_warps ? tu.target_warps : kDefaultTargetWarps;
   const int min_piece = tu.min_piece ? tu.min_piece : kDefaultMinPiece;
   const int LG = 32 / WB;
@@ -885,8 +997,14 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu)
     }
     const int fsplit = (int)std::max<int64_t>(1, (target_warps + nfw - 1) / std::max<int64_t>(nfw, 1));
     const int bsplit = (int)std::max<int64_t>(1, (target_warps + nbw - 1) / std::max<int64_t>(nbw, 1));
+    const bool pack_level = pack_rows > 0 && nfw >= pack_min_warps;
+    std::vector<int> packable;
     for (int s : by_level[l]) {
       const int k = F.sn_k[s], nf = k + F.sn_m[s], c0 = F.sn_col0[s];
+      if (pack_level && nf <= pack_rows && k <= kPackMaxK && F.sn_rowptr[s] < INT32_MAX) {
+        packable.push_back(s);   // the whole supernode in one lane
+        continue;
+      }
       bool zf_s = false, zb_s = false;
       const int fplen = pieces_of(k, fsplit);
       for (int r0 = 0; r0 < nf; r0 += RPI_f) {
@@ -909,6 +1027,40 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu)
       if (zf_s) for (int i = 0; i < k; ++i) S.zf.push_back(c0 + i);
       if (zb_s) for (int i = 0; i < k; ++i) S.zb.push_back(c0 + i);
     }
+    // similar shapes share a pack (little padding)
+    std::stable_sort(packable.begin(), packable.end(), [&](int a, int c) {
+      return std::make_pair(F.sn_k[a], F.sn_m[a]) < std::make_pair(F.sn_k[c], F.sn_m[c]);
+    });
+    for (size_t i = 0; i < packable.size(); i += 32) {
+      const int count = (int)std::min<size_t>(32, packable.size() - i);
+      int NP = 0, KP = 0;
+      for (int l = 0; l < count; ++l) {
+        const int t = packable[i + l];
+        NP = std::max(NP, F.sn_k[t] + F.sn_m[t]);
+        KP = std::max(KP, F.sn_k[t]);
+      }
+      const int64_t p = (int64_t)S.pack_sn.size() / 32, off = (int64_t)S.pack_vals.size() / 32;
+      if (p >= INT32_MAX || off >= INT32_MAX) throw Error(JJA_ERR_ARG, "too many packed supernodes");
+      S.pack_vals.resize(S.pack_vals.size() + (size_t)32 * NP * KP, 0.0);
+      double* vals = S.pack_vals.data() + off * 32;
+      for (int l = 0; l < 32; ++l) {
+        if (l >= count) {
+          S.pack_sn.push_back(-1);
+          S.pack_meta.push_back(make_int4(0, 0, 0, 0));
+          continue;
+        }
+        const int t = packable[i + l], k = F.sn_k[t], nf = k + F.sn_m[t];
+        S.pack_sn.push_back(t);
+        S.pack_meta.push_back(make_int4(F.sn_col0[t], k, nf, (int)F.sn_rowptr[t]));
+        const double* Fs = F.fcol.data() + F.sn_valptr[t];
+        for (int j = 0; j < k; ++j)
+          for (int r = 0; r < nf; ++r) vals[((int64_t)j * NP + r) * 32 + l] = Fs[(int64_t)j * nf + r];
+      }
+      const int4 item = make_int4((int)(-1 - p), count, NP | (KP << 16), (int)off);
+      S.fi.push_back(item);
+      S.bi.push_back(item);
+    }
+    S.level_packed.push_back(!packable.empty());
     S.fwd_ptr.push_back((int64_t)S.fi.size());
     S.bwd_ptr.push_back((int64_t)S.bi.size());
   }
@@ -916,8 +1068,8 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu)
     S.bi_flow.insert(S.bi_flow.end(), S.bi.begin() + S.bwd_ptr[l], S.bi.begin() + S.bwd_ptr[l + 1]);
   const int ns = F.ns;
   std::vector<uint32_t> nfi(ns, 0), nbi(ns, 0);
-  for (const int4& v : S.fi) nfi[v.x]++;
-  for (const int4& v : S.bi) nbi[v.x]++;
+  for (const int4& v : S.fi) for_each_supernode(S, v, [&](int s) { nfi[s]++; });
+  for (const int4& v : S.bi) for_each_supernode(S, v, [&](int s) { nbi[s]++; });
   S.fcnt.assign(ns, 0);
   S.bcnt.assign(ns, 0);
   S.fon.assign(ns, -1);
@@ -949,14 +1101,15 @@ void check_schedule(const Schedule& S) {
     std::vector<int64_t> first(ns, INT64_MAX), last_notifier(ns, -1);
     std::vector<uint32_t> notifiers(ns, 0);
     for (int64_t i = 0; i < (int64_t)items.size(); ++i) {
-      const int s = items[i].x;
-      if (s < 0 || s >= ns) throw Error(JJA_ERR_INTERNAL, std::string(which) + ": item supernode out of range");
-      first[s] = std::min(first[s], i);
-      const int t = notify[s];
-      if (t >= 0) {
-        last_notifier[t] = i;
-        notifiers[t]++;
-      }
+      for_each_supernode(S, items[i], [&](int s) {
+        if (s < 0 || s >= ns) throw Error(JJA_ERR_INTERNAL, std::string(which) + ": item supernode out of range");
+        first[s] = std::min(first[s], i);
+        const int t = notify[s];
+        if (t >= 0) {
+          last_notifier[t] = i;
+          notifiers[t]++;
+        }
+      });
     }
     for (int s = 0; s < ns; ++s) {
       const int t = on[s];
@@ -986,6 +1139,7 @@ struct jja_plan {
   FactorDev F{};
   std::vector<void*> allocs;
   std::vector<int64_t> fwd_ptr, bwd_ptr;
+  std::vector<char> level_packed;
   int4* fwd_items = nullptr;
   int4* bwd_items = nullptr;        // levels ascending (level launches index them per level)
   int4* bwd_flow_items = nullptr;   // the same items root first (dataflow sweep order)
@@ -1099,14 +1253,16 @@ void launch_sweep(jja_plan* p, cudaStream_t st, bool forward, double* b, double*
     for (int l = 0; l < p->n_levels; ++l) {
       const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
       if (!n) continue;
-      launch(p->pdl, k_fwd_level<RPL>, (n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, st, p->F,
+      launch(p->pdl, p->level_packed[l] ? k_fwd_level<RPL, true> : k_fwd_level<RPL, false>,
+             (n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, st, p->F,
              (const int4*)(p->fwd_items + p->fwd_ptr[l]), n, p->W, p->WB, b, z);
     }
   } else {        // levels descending; x produced
     for (int l = p->n_levels - 1; l >= 0; --l) {
       const int n = (int)(p->bwd_ptr[l + 1] - p->bwd_ptr[l]);
       if (!n) continue;
-      launch(p->pdl, k_bwd_level<RPL>, (n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, st, p->F,
+      launch(p->pdl, p->level_packed[l] ? k_bwd_level<RPL, true> : k_bwd_level<RPL, false>,
+             (n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, st, p->F,
              (const int4*)(p->bwd_items + p->bwd_ptr[l]), n, p->W, p->WB, (const double*)z, x);
     }
   }
@@ -1454,9 +1610,12 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->n_levels = S.n_levels;
     p->fwd_ptr = S.fwd_ptr;
     p->bwd_ptr = S.bwd_ptr;
+    p->level_packed = S.level_packed;
     p->fwd_items = p->up(S.fi.data(), S.fi.size());
     p->bwd_items = p->up(S.bi.data(), S.bi.size());
     p->bwd_flow_items = p->up(S.bi_flow.data(), S.bi_flow.size());
+  p->F.pack_meta = p->up(S.pack_meta.data(), S.pack_meta.size());
+  p->F.pack_vals = p->up(S.pack_vals.data(), S.pack_vals.size());
     p->nz_f = (int)S.zf.size();
     p->nz_b = (int)S.zb.size();
     p->zrows_f = p->up(S.zf.data(), S.zf.size());

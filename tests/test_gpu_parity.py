@@ -54,6 +54,24 @@ def test_face_solve_matches_scipy(make, W):
     close(x, ref, rtol=1e-11)
 
 
+@pytest.mark.parametrize("make", [lambda: SquareArray(60, 47), lambda: HoneycombArray(25, 21),
+                                  lambda: TriangularArray(33, 40)])
+@pytest.mark.parametrize("ordering", ["nd", "mmd"])
+@pytest.mark.parametrize("pack_rows", [0, 8, 48])
+def test_face_solve_w1_packs(make, ordering, pack_rows):
+    """W = 1 packs of small supernodes (one per lane, interleaved values) on every level where
+    they fit (pack_min_warps 1): the solve against scipy, and against the same plan without packs."""
+    c = make()
+    c.set_inductance(0.05)
+    A, K = P.face_matrix(c, 0.05)
+    b = np.random.default_rng(pack_rows).standard_normal(K.shape[0])
+    ref = scipy.sparse.linalg.spsolve(K.tocsc(), b)
+    x = backend.solve_faces(c, 0.05, b, ordering=ordering, tuning={"pack_rows": pack_rows, "pack_min_warps": 1})
+    x0 = backend.solve_faces(c, 0.05, b, ordering=ordering, tuning={"pack_rows": -1})
+    close(x, ref, rtol=1e-11)
+    close(x, x0, rtol=1e-12)
+
+
 def _mixed_problem(c, W, Nt, seed):
     rng = np.random.default_rng(seed)
     Nj, Nf = c.junction_count(), c.face_count()
@@ -74,6 +92,19 @@ def test_against_oracle(make, W):
     prob = _mixed_problem(c, W, 300, W)
     th_o, I_o, V_o = rcsj_oracle.time_evolution(prob)
     res = prob.compute()
+    close(res.get_theta(), th_o)
+    close(res.get_current(), I_o)
+    close(res.get_voltage(), V_o, rtol=1e-8)
+
+
+def test_w1_packs_against_oracle():
+    """One problem (W = 1) with packs on every level where they fit, against the oracle."""
+    c = SquareArray(31, 26)
+    c.set_capacitance(0.3)
+    c.set_inductance(0.2)
+    prob = _mixed_problem(c, 1, 300, 11)
+    th_o, I_o, V_o = rcsj_oracle.time_evolution(prob)
+    res = prob.compute(tuning={"pack_min_warps": 1}, ordering="mmd")
     close(res.get_theta(), th_o)
     close(res.get_current(), I_o)
     close(res.get_voltage(), V_o, rtol=1e-8)

@@ -101,7 +101,9 @@ def test_plan_create_without_gpu_reports_cuda_error():
 @pytest.mark.parametrize("make", [lambda: SquareArray(128, 128), lambda: HoneycombArray(20, 17),
                                   lambda: TriangularArray(30, 21), lambda: SquareArray(7, 5)])
 @pytest.mark.parametrize("ordering", ["nd", "mmd"])
-@pytest.mark.parametrize("W,tuning", [(1, None), (8, {"rows_per_lane": 8}), (64, {"rhs_block": 16}),
+@pytest.mark.parametrize("W,tuning", [(1, None), (1, {"pack_rows": -1}), (1, {"pack_min_warps": 1}),
+                                      (1, {"pack_rows": 64, "pack_min_warps": 1}),
+                                      (8, {"rows_per_lane": 8}), (64, {"rhs_block": 16}),
                                       (512, None), (512, {"rows_per_lane": 2, "min_piece": 4,
                                                           "target_warps": 152 * 200}), (3, {"schedule": 2})])
 def test_dataflow_schedule_waits_only_on_earlier_items(make, ordering, W, tuning):
@@ -114,7 +116,14 @@ def test_dataflow_schedule_waits_only_on_earlier_items(make, ordering, W, tuning
     coords, perm = P.fill_reducing_order(K, ordering, c)
     f = P.HostFactor(K, coords=coords, perm=perm)
     nf, nb = f.check_schedule(W, tuning)
-    assert nf >= f.stats["n_supernodes"] and nb >= f.stats["n_supernodes"]
+    ns = f.stats["n_supernodes"]
+    # a W = 1 pack holds up to 32 small supernodes; otherwise every supernode has >= 1 item
+    packed = W == 1 and (tuning or {}).get("pack_rows", 0) >= 0
+    least = -(-ns // 32) if packed else ns
+    assert nf >= least and nb >= least
+    if packed and (tuning or {}).get("pack_min_warps") == 1 and ns > 64:   # packs on every level
+        nf1, nb1 = f.check_schedule(W, {"pack_rows": -1})
+        assert nf < nf1 and nb < nb1
 
 
 def test_ctypes_structs_match_the_header():
