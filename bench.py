@@ -467,7 +467,9 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling mode: plan, 3 eager warm-up steps, then this many eager steps, nothing else")
     ap.add_argument("--W", type=int, default=W_BATCH, help="problems per launch (profiling mode)")
-    ap.add_argument("--ordering", default="nd", choices=["nd", "mmd"], help="fill-reducing order of the factor")
+    ap.add_argument("--ordering", default="auto", choices=["auto", "nd", "mmd"],
+                    help="fill-reducing order of the factor (auto: minimum degree when W x Nf >= 2^22 on up to "
+                         "2^18 faces, else nested dissection)")
     ap.add_argument("--relax", default="-1,-1", help="supernode amalgamation: max zeros,max fraction (-1: default)")
     ap.add_argument("--adjoint-steps", type=int, default=5000,
                     help="time steps of the adjoint-cost leg (0 skips it)")

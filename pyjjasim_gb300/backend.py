@@ -158,7 +158,7 @@ class GpuSimulation:
     ``run_timed`` advances with per-stage CUDA-event timing, ``theta`` returns the newest phase.
     """
 
-    def __init__(self, problem, noise="philox", seed=None, device=None, nd_leaf=8, stream=None, ordering="nd",
+    def __init__(self, problem, noise="philox", seed=None, device=None, nd_leaf=8, stream=None, ordering="auto",
                  relax=(-1, -1.0), Ic=None, tuning=None, tune=False):
         """``Ic``: optional (Nj, W) critical currents per problem, replacing the circuit's
         (problems then differ in Ic but share the face-space matrix, which does not depend on Ic).
@@ -179,11 +179,11 @@ class GpuSimulation:
                 from .autotune import autotune
                 opts = autotune(c, problem._dt(), self.W, self.width, nd_leaf=nd_leaf, device=self.dev.index)
                 ordering, relax, tuning = opts["ordering"], opts["relax"], opts["tuning"]
-            self.ordering = ordering
+            self.ordering = P.resolve_ordering(ordering, self.W, self.Nf)
             self.relax, self.tuning = tuple(relax), dict(tuning or {})
             self.stream = stream if stream is not None else torch.cuda.Stream(device=self.dev)
             self.plan = P.get_plan(c, problem._dt(), self.W, self.width, problem.stencil, nd_leaf=nd_leaf,
-                                   ordering=ordering, relax=relax, Ic_w=Ic, tuning=tuning)
+                                   ordering=self.ordering, relax=relax, Ic_w=Ic, tuning=tuning)
             hist0 = [problem.config_at_minus_1, problem.config_at_minus_2]
             if self.width >= 4:
                 hist0.append(problem.config_at_minus_3)
@@ -355,11 +355,12 @@ class GpuSimulation:
 
 
 def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", seed=None, device=None,
-                        use_graph=True, nd_leaf=8, stream=None, ordering="nd", relax=(-1, -1.0), Ic=None,
+                        use_graph=True, nd_leaf=8, stream=None, ordering="auto", relax=(-1, -1.0), Ic=None,
                         tuning=None, tune=False):
     """GPU time-stepping core; see the module docstring for the contract.
 
-    ``ordering`` ("nd" or "mmd") and ``relax`` ((max zeros, max fraction) of supernode
+    ``ordering`` ("nd", "mmd" or "auto": minimum degree when W x Nf >= 2^22 on up to 2^18 faces,
+    nested dissection otherwise) and ``relax`` ((max zeros, max fraction) of supernode
     amalgamation; negative = library defaults) select how the face-space matrix is factorised;
     ``tuning`` the solve's launch shape; ``tune=True`` lets the autotuner pick both."""
     sim = GpuSimulation(problem, noise=noise, seed=seed, device=device, nd_leaf=nd_leaf, stream=stream,
@@ -410,7 +411,7 @@ def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", se
     return th_buf.transpose(1, 2, 0), I_buf.transpose(1, 2, 0)
 
 
-def solve_faces(circuit, dt, b, stencil_width=3, nd_leaf=8, ordering="nd", tuning=None):
+def solve_faces(circuit, dt, b, stencil_width=3, nd_leaf=8, ordering="auto", tuning=None):
     """K^{-1} b on the GPU for (Nf, W) right-hand sides (the per-step face-space solve);
     ``ordering`` and ``tuning`` as for the simulation's plan."""
     from .problem import stencil

@@ -85,6 +85,16 @@ def test_nested_dissection_fill_is_bounded():
     assert st["n_levels"] <= 30
 
 
+def test_auto_ordering_policy():
+    # minimum degree only where the step is FP64-bound (lots of face-problems) and SuperLU's
+    # host ordering run stays cheap; explicit orderings pass through
+    assert P.resolve_ordering("auto", 512, 127 * 127) == "mmd"
+    assert P.resolve_ordering("auto", 64, 63 * 63) == "nd"
+    assert P.resolve_ordering("auto", 1, 255 * 255) == "nd"
+    assert P.resolve_ordering("auto", 8, 1023 * 1023) == "nd"
+    assert P.resolve_ordering("nd", 512, 127 * 127) == "nd" and P.resolve_ordering("mmd", 1, 10) == "mmd"
+
+
 def test_plan_create_without_gpu_reports_cuda_error():
     # creating a device plan must fail loudly (no CPU fallback) when no GPU is present
     import torch
