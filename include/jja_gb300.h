@@ -266,9 +266,16 @@ int jja_solve_static(jja_plan* p, const double* b, double* x, void* stream);
 int jja_vortex(jja_plan* p, const double* theta, int64_t n_steps, int32_t* n_out, uint64_t* flow, void* stream);
 
 /* out[i] = sin(x[i]) with the library's device sine (device arrays of n doubles), the one
- * the junction-current kernels use for Ic sin(theta) (pyjjasim static_problem.py:82-85).
- * Exposed so tests can bound its error against a correctly rounded sine. */
+ * the junction-current kernels use for Ic sin(theta) (pyjjasim static_problem.py:82-85): 64-bit
+ * fixed point and FP32, no FP64 instruction; within 1.2e-16 of a correctly rounded sine for
+ * |x| < 2^62, NaN from 2^62 on. Exposed so tests can bound its error. */
 int jja_eval_sin(jja_plan* p, const double* x, double* out, int64_t n, void* stream);
+
+/* The same sine (and the cosine the adjoint uses) evaluated on the host by the same source code
+ * (64-bit fixed point and FP32, no GPU needed): s[i] = sin(x[i]), c[i] = cos(x[i]) for host
+ * arrays of n doubles; either output may be NULL. A diagnostic: tests check the algorithm's
+ * error on the CPU over many more points than a GPU run needs. */
+int jja_sin_host(const double* x, double* s, double* c, int64_t n);
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* jja_last_error(void);

@@ -88,6 +88,7 @@ SIGNATURES = {
     "jja_adjoint_flux": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "jja_vortex": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "jja_eval_sin": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
+    "jja_sin_host": (c_int, [P_f64, P_f64, P_f64, c_int64]),
     "jja_last_error": (ctypes.c_char_p, []),
     "jja_launch_count": (c_int64, []),
 }

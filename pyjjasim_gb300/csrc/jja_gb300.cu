@@ -158,26 +158,8 @@ struct Tables {
   const int32_t* fj_ell;   // faces of <= kEllMax junctions: Nf x face_deg codes, padded with -1
   int face_deg;            // 0 when some face has more than kEllMax junctions (CSR path)
   const int32_t* jf_face;  // 2 per junction: (permuted face << 1) | (A entry is -1), or -1
-  const double2* sincos;   // per k < 65536: {S, C} = {sin, cos}(k pi/32768)
+  const longlong2* sincos; // per k < 65536: {S, C} = {sin, cos}(k pi/32768) in units of 2^-62
 };
-
-// FP64 <-> FP32 conversions by bit manipulation on the integer pipe: on GB300 the conversion
-// instructions share the narrow FP64 pipe. Valid for |v| in [2^-126, 2^128); smaller values
-// flush to signed zero (callers only convert small correction terms).
-__device__ __forceinline__ float f32_from_f64(double v) {
-  const unsigned hi = (unsigned)__double2hiint(v), lo = (unsigned)__double2loint(v);
-  const int e = (int)((hi >> 20) & 0x7ffu);
-  unsigned bits = (hi & 0x80000000u) | ((unsigned)(e - 896) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
-  bits += (lo >> 28) & 1u;                    // round half away from zero on the magnitude
-  return __uint_as_float((e > 896 && e < 1151) ? bits : (hi & 0x80000000u));
-}
-
-__device__ __forceinline__ double f64_from_f32(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xffu;
-  const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
-  return e ? __hiloint2double((int)hi, (int)(b << 29)) : 0.0;
-}
 
 // +-v by flipping the sign bit (no FP64 instruction)
 __device__ __forceinline__ double signed_by(double v, int neg) {
@@ -185,58 +167,202 @@ __device__ __forceinline__ double signed_by(double v, int neg) {
 }
 
 // ------------------------------------------------------------------------------------------
-// sin(x) in FP64 with few FP64 instructions (GB300's FP64 pipe is ~60x narrower than FP32).
-// Cody-Waite reduction x = k pi/32768 + t, |t| <= pi/65536 = 4.8e-5, with two constants:
-// C1 = pi/32768 rounded to double, C2 = (pi/32768 - C1) rounded. fma(-k, C1, x) is exact for
-// |x| < 2e5: k C1 and x are multiples of 2^-67 there and their difference is below 2^-14, so it
-// fits in 52 bits; the second FMA adds one rounding of <= 2^-69 and the constants' own error
-// is < 2^-120 k. Then
-//   sin(x) = S + C t - S t^2/2 - C t^3/6 + O(t^4),  S, C = sin, cos(k pi/32768),
-// from a 65536-entry table (1 MB, L2-resident) computed on the host in extended precision.
-// |S t^2/2| < 1.2e-9 and |t^3/6| < 1.9e-14, so both terms are evaluated in FP32 (absolute
-// error < 1e-16, checked by exact emulation and on the GPU); S + C t is one FP64 FMA and the
-// O(t^4) remainder is below 3e-19. |x| >= 2e5, inf and NaN fall back to the CUDA math library
-// (range test on the integer pipe). Six FP64 instructions in all.
+// sin(x) and cos(x) to FP64 accuracy without FP64 instructions. GB300's FP64 pipe is ~60x
+// narrower than its FP32 and integer pipes, and the junction kernels are bound by it; this
+// evaluation runs on the integer pipe (64-bit fixed point) with an FP32 correction term.
+// Table-driven method (Tang, ACM TOMS 15(2), 1989) with an exact Payne-Hanek style reduction:
+// 1. |x| = M 2^(e-1075) exactly (M: the 53-bit significand). u = |x| 2^15/pi is formed as M times
+//    2^15/pi held to 128 bits (kInvPiHi:kInvPiLo = floor(2^129/pi), computed to 400 bits with
+//    mpmath), keeping 64 fractional bits of u and the low bits of its integer part (error
+//    < |x| 2^-114 in u: below 2^-70 for the phases' range, 2^-52 at |x| = 2^62). k = nearest
+//    integer to u, f = u - k in [-1/2, 1/2], t = f pi/2^15 (|t| <= 4.8e-5) as a signed 64-bit
+//    number in units of 2^-76 (kPi61 = round(pi 2^61)).
+// 2. With S, C = sin, cos(k pi/32768) from a 65536-entry table in units of 2^-62 (1 MB,
+//    L2-resident, computed on the host in extended precision):
+//      sin(|x|) = S + C t - S t^2/2 - C t^3/6,   cos(x) = C - S t - C t^2/2 + S t^3/6,
+//    remainder below 3e-19. S + C t and the quadratic term are formed in fixed point (64x64-bit
+//    products), the cubic term (< 1.9e-14) in FP32 (absolute error < 2e-21).
+// 3. The fixed-point sum (absolute error ~1e-18) is rounded to the nearest double with integer
+//    operations (count of leading zeros, shift, round half to even).
+// |x| < 2^-27 gives sin = x, cos = 1 (the next terms are below half an ulp); |x| >= 2^62, inf
+// and NaN give NaN. No library call: the kernels keep no stack frame for one. Host and device
+// share this code, so the library can check it on the CPU (jja_sin_host).
 // ------------------------------------------------------------------------------------------
-constexpr double kSinScale = 0x1.45f306dc9c883p+13;  // 32768 / pi
-constexpr double kSinC1 = 0x1.921fb54442d18p-14;     // pi/32768 rounded to double
-constexpr double kSinC2 = 0x1.1a62633145c07p-68;     // pi/32768 - kSinC1, rounded
-constexpr double kRoundMagic = 6755399441055744.0;   // 1.5 * 2^52: adding it rounds to an integer
 constexpr int kSinTable = 65536;
+constexpr uint64_t kInvPiHi = 0xa2f9836e4e441529ull;   // floor(2^15/pi 2^114) = kInvPiHi 2^64 + kInvPiLo
+constexpr uint64_t kInvPiLo = 0xfc2757d1f534ddc0ull;
+constexpr int64_t kPi61 = 0x6487ed5110b4611all;       // round(pi 2^61)
 
-__device__ __forceinline__ double fast_sin(double x, const double2* __restrict__ tab) {
-  if ((__double2hiint(x) & 0x7fffffff) >= 0x41086A00) return sin(x);   // |x| >= 2e5, inf, NaN
-  const double s = fma(x, kSinScale, kRoundMagic);
-  const int k = __double2loint(s) & (kSinTable - 1);
-  const double kd = s - kRoundMagic;
-  const double t = fma(-kd, kSinC2, fma(-kd, kSinC1, x));
-  const double2 sc = __ldg(tab + k);           // S, C
-  const double r = fma(sc.y, t, sc.x);         // S + C t
-  const float tf = f32_from_f64(t), sf = f32_from_f64(sc.x), cf = f32_from_f64(sc.y);
-  const float t2 = tf * tf;
-  const float tail = fmaf(-0.5f * sf, t2, (-(1.0f / 6.0f) * cf) * (t2 * tf));   // -S t^2/2 - C t^3/6
-  return r + f64_from_f32(tail);
+__host__ __device__ __forceinline__ uint64_t umulhi64(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
 }
 
-// sin and cos from one reduction: cos(a + t) = C - S t - C t^2/2 + S t^3/6 + O(t^4)
-__device__ __forceinline__ void fast_sincos(double x, const double2* __restrict__ tab, double& s_out, double& c_out) {
-  if ((__double2hiint(x) & 0x7fffffff) >= 0x41086A00) {
-    sincos(x, &s_out, &c_out);
+__host__ __device__ __forceinline__ int64_t smulhi64(int64_t a, int64_t b) {
+#ifdef __CUDA_ARCH__
+  return __mul64hi(a, b);
+#else
+  return (int64_t)(((__int128)a * b) >> 64);
+#endif
+}
+
+__host__ __device__ __forceinline__ uint64_t bits_of(double v) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(v);
+#else
+  uint64_t b;
+  memcpy(&b, &v, 8);
+  return b;
+#endif
+}
+
+__host__ __device__ __forceinline__ double double_of(uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double v;
+  memcpy(&v, &b, 8);
+  return v;
+#endif
+}
+
+__host__ __device__ __forceinline__ float float_of_int(int v) {
+#ifdef __CUDA_ARCH__
+  return __int2float_rn(v);
+#else
+  return (float)v;
+#endif
+}
+
+// f 2^62 truncated to an integer, for |f| < 2^-28 (the cubic terms)
+__host__ __device__ __forceinline__ int64_t fixed62_of_float(float f) {
+  uint32_t b;
+#ifdef __CUDA_ARCH__
+  b = __float_as_uint(f);
+#else
+  memcpy(&b, &f, 4);
+#endif
+  const int E = (int)((b >> 23) & 0xffu);
+  const int64_t m = (int64_t)((b & 0x7fffffu) | 0x800000u);
+  const int sh = E - 88;   // f 2^62 = m 2^(E - 150 + 62)
+  const int64_t v = E == 0 ? 0 : sh >= 0 ? (m << sh) : (sh > -64 ? (m >> -sh) : 0);
+  return (b >> 31) ? -v : v;
+}
+
+// R 2^-62 rounded to the nearest double, negated when `neg`
+__host__ __device__ __forceinline__ double double_of_fixed62(int64_t R, bool neg) {
+  const bool sign = (R < 0) != neg;
+  const uint64_t a = R < 0 ? (uint64_t)0 - (uint64_t)R : (uint64_t)R;
+  if (a == 0) return double_of((uint64_t)neg << 63);
+#ifdef __CUDA_ARCH__
+  const int lz = __clzll((long long)a);
+#else
+  const int lz = __builtin_clzll(a);
+#endif
+  const uint64_t n = a << lz;                     // leading one at bit 63
+  uint64_t mant = n >> 11;                        // 53 bits
+  const uint64_t rem = n & 0x7ffu;
+  mant += (rem > 0x400u) || (rem == 0x400u && (mant & 1u));
+  // value in [2^(1-lz), 2^(2-lz)): biased exponent 1024 - lz; a carry out of the rounding
+  // moves into the exponent field
+  return double_of((((uint64_t)(1023 - lz) << 52) + mant) | ((uint64_t)sign << 63));
+}
+
+struct SinReduced {
+  unsigned idx;    // k mod 65536
+  int64_t t;       // t in units of 2^-76
+};
+
+// 64 bits of the 192-bit number (P2 P1 P0) starting at bit `pos` (0 <= pos), zeros above bit 191
+__host__ __device__ __forceinline__ uint64_t bits_at(uint64_t P0, uint64_t P1, uint64_t P2, int pos) {
+  if (pos >= 192) return 0;
+  if (pos >= 128) return P2 >> (pos - 128);
+  if (pos == 64) return P1;
+  if (pos > 64) return (P1 >> (pos - 64)) | (P2 << (128 - pos));
+  if (pos == 0) return P0;
+  return (P0 >> pos) | (P1 << (64 - pos));
+}
+
+// step 1 for 2^-27 <= |x| < 2^62 (biased exponent e in [996, 1084])
+__host__ __device__ __forceinline__ SinReduced sin_reduce(uint64_t ax) {
+  const int e = (int)(ax >> 52);
+  const uint64_t M = (ax & 0xfffffffffffffull) | (1ull << 52);
+  // P = M (kInvPiHi 2^64 + kInvPiLo), 181 bits
+  const uint64_t P0 = M * kInvPiLo, a_hi = umulhi64(M, kInvPiLo);
+  const uint64_t b_lo = M * kInvPiHi, b_hi = umulhi64(M, kInvPiHi);
+  const uint64_t P1 = a_hi + b_lo;
+  const uint64_t P2 = b_hi + (P1 < a_hi ? 1u : 0u);
+  // u 2^64 = P 2^(e - 1125): fraction = bits [sh, sh + 64) of P, integer part above (only its
+  // low 16 bits index the table)
+  const int sh = 1125 - e;   // 41 .. 129
+  const uint64_t frac = bits_at(P0, P1, P2, sh);
+  const uint64_t kint = bits_at(P0, P1, P2, sh + 64);
+  SinReduced r;
+  r.idx = (unsigned)(kint + (frac >> 63)) & (unsigned)(kSinTable - 1);   // round to nearest
+  r.t = smulhi64((int64_t)frac, kPi61);   // f 2^64 pi 2^61 2^-64 = t 2^76
+  return r;
+}
+
+// steps 2 and 3: sin(|x|) and cos(x) from the reduction and the table entry {S, C} (2^-62
+// units). t^2 is formed in units of 2^-88; the cubic term (< 1.9e-14) in FP32.
+__host__ __device__ __forceinline__ int64_t sin_fixed(const SinReduced& r, longlong2 sc) {
+  const int64_t ct = (smulhi64(sc.y, r.t) + (1 << 11)) >> 12;         // C t
+  const int64_t t2 = smulhi64(r.t, r.t);                               // t^2 2^88
+  const int64_t st2 = (smulhi64(sc.x, t2) + (1 << 24)) >> 25;          // S t^2 / 2
+  const float tf = float_of_int((int)(r.t >> 32)) * 0x1p-44f, cf = float_of_int((int)(sc.y >> 32)) * 0x1p-30f;
+  const float cubic = (-(1.0f / 6.0f) * cf) * (tf * tf * tf);          // -C t^3/6
+  return sc.x + ct - st2 + fixed62_of_float(cubic);
+}
+
+__host__ __device__ __forceinline__ int64_t cos_fixed(const SinReduced& r, longlong2 sc) {
+  const int64_t st = (smulhi64(sc.x, r.t) + (1 << 11)) >> 12;         // S t
+  const int64_t t2 = smulhi64(r.t, r.t);
+  const int64_t ct2 = (smulhi64(sc.y, t2) + (1 << 24)) >> 25;          // C t^2 / 2
+  const float tf = float_of_int((int)(r.t >> 32)) * 0x1p-44f, sf = float_of_int((int)(sc.x >> 32)) * 0x1p-30f;
+  const float cubic = ((1.0f / 6.0f) * sf) * (tf * tf * tf);           // S t^3/6
+  return sc.y - st - ct2 + fixed62_of_float(cubic);
+}
+
+__host__ __device__ __forceinline__ longlong2 sin_table_entry(const longlong2* tab, unsigned idx) {
+#ifdef __CUDA_ARCH__
+  return __ldg(tab + idx);
+#else
+  return tab[idx];
+#endif
+}
+
+// |x| >= 2^62 (where x carries no information modulo 2 pi), inf and NaN give NaN
+__host__ __device__ __forceinline__ bool sin_outside_range(uint64_t ax) { return ax >= (1085ull << 52); }
+__host__ __device__ __forceinline__ bool sin_tiny(uint64_t ax) { return ax < (996ull << 52); }   // |x| < 2^-27
+constexpr uint64_t kNaNBits = 0x7ff8000000000000ull;
+
+__host__ __device__ __forceinline__ double fast_sin(double x, const longlong2* __restrict__ tab) {
+  const uint64_t xb = bits_of(x), ax = xb & 0x7fffffffffffffffull;
+  if (sin_outside_range(ax)) return double_of(kNaNBits);
+  if (sin_tiny(ax)) return x;
+  const SinReduced r = sin_reduce(ax);
+  return double_of_fixed62(sin_fixed(r, sin_table_entry(tab, r.idx)), (xb >> 63) != 0);
+}
+
+__host__ __device__ __forceinline__ void fast_sincos(double x, const longlong2* __restrict__ tab, double& s_out,
+                                                     double& c_out) {
+  const uint64_t xb = bits_of(x), ax = xb & 0x7fffffffffffffffull;
+  if (sin_outside_range(ax)) {
+    s_out = c_out = double_of(kNaNBits);
     return;
   }
-  const double s = fma(x, kSinScale, kRoundMagic);
-  const int k = __double2loint(s) & (kSinTable - 1);
-  const double kd = s - kRoundMagic;
-  const double t = fma(-kd, kSinC2, fma(-kd, kSinC1, x));
-  const double2 sc = __ldg(tab + k);           // S, C
-  const double rs = fma(sc.y, t, sc.x);        // S + C t
-  const double rc = fma(-sc.x, t, sc.y);       // C - S t
-  const float tf = f32_from_f64(t), sf = f32_from_f64(sc.x), cf = f32_from_f64(sc.y);
-  const float t2 = tf * tf, t3 = t2 * tf;
-  const float ts = fmaf(-0.5f * sf, t2, (-(1.0f / 6.0f) * cf) * t3);
-  const float tc = fmaf(-0.5f * cf, t2, ((1.0f / 6.0f) * sf) * t3);
-  s_out = rs + f64_from_f32(ts);
-  c_out = rc + f64_from_f32(tc);
+  if (sin_tiny(ax)) {
+    s_out = x;
+    c_out = 1.0;
+    return;
+  }
+  const SinReduced r = sin_reduce(ax);
+  const longlong2 sc = sin_table_entry(tab, r.idx);
+  s_out = double_of_fixed62(sin_fixed(r, sc), (xb >> 63) != 0);
+  c_out = double_of_fixed62(cos_fixed(r, sc), false);
 }
 
 // q(j, w) = x / c0 for the step whose phase history is th[0..] (time_evolution.py:533-558):
@@ -358,8 +484,11 @@ __global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const do
 // theta_next = (A^T J)/c0 - q, outputs, theta_s update (time_evolution.py:562-580); with
 // `fuse_next` the same thread then evaluates q of the next step from the new history
 // (theta_next, h[0], ...), saving a pass over the phase arrays.
+#ifndef JJA_UPDATE_MIN_BLOCKS
+#define JJA_UPDATE_MIN_BLOCKS 6   // resident blocks per SM the register allocation must allow (measured: 4 -> 6 is 16 % faster)
+#endif
 template <bool kFuseNext>
-__global__ void __launch_bounds__(256) k_update(StepArgs a, Tables t, double* __restrict__ q,
+__global__ void __launch_bounds__(256, JJA_UPDATE_MIN_BLOCKS) k_update(StepArgs a, Tables t, double* __restrict__ q,
                                                 const double* __restrict__ J) {
   pdl_begin();
   const int64_t NjW = (int64_t)a.Nj * a.W;
@@ -859,7 +988,7 @@ __global__ void k_unpermute_scaled(const double* __restrict__ src, double* __res
 }
 
 __global__ void k_eval_sin(const double* __restrict__ x, double* __restrict__ out, int64_t n,
-                           const double2* __restrict__ tab) {
+                           const longlong2* __restrict__ tab) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     out[i] = fast_sin(x[i], tab);
 }
@@ -1122,6 +1251,27 @@ void check_schedule(const Schedule& S) {
   };
   check(S.fi, S.fon, S.fcnt, S.fnot, "forward schedule");
   check(S.bi_flow, S.bon, S.bcnt, S.bnot, "backward schedule");
+}
+
+}  // namespace
+
+namespace {
+
+// {sin, cos}(k pi/32768) in units of 2^-62: first-quadrant values in extended precision,
+// rounded once, then exact quadrant symmetries (sin(m pi) and cos(m pi + pi/2) are exactly 0)
+std::vector<longlong2> build_sin_table() {
+  std::vector<longlong2> tab((size_t)kSinTable);
+  const long double pi_l = 3.141592653589793238462643383279502884L;
+  const long double scale = 4611686018427387904.0L;   // 2^62
+  const int quarter = kSinTable / 4;
+  for (int k = 0; k < kSinTable; ++k) {
+    const int q = k / quarter, r = k % quarter;
+    const long double ang = (long double)r * pi_l / (long double)(kSinTable / 2);
+    const long long s0 = llroundl(sinl(ang) * scale), c0 = llroundl(cosl(ang) * scale);
+    const long long sv[4] = {s0, c0, -s0, -c0}, cv[4] = {c0, -s0, -c0, s0};
+    tab[(size_t)k] = make_longlong2(sv[q], cv[q]);
+  }
+  return tab;
 }
 
 }  // namespace
@@ -1573,18 +1723,7 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->t.jf_face = p->up(jf_face.data(), jf_face.size());
     p->perm = p->up(F.perm.data(), F.perm.size());
     {
-      // {sin, cos}(k pi/32768): first-quadrant values in extended precision, rounded once to
-      // double, then exact quadrant symmetries, so sin(m pi) and cos(m pi + pi/2) are exactly 0
-      std::vector<double2> tab((size_t)kSinTable);
-      const long double pi_l = 3.141592653589793238462643383279502884L;
-      const int quarter = kSinTable / 4;
-      for (int k = 0; k < kSinTable; ++k) {
-        const int q = k / quarter, r = k % quarter;
-        const long double ang = (long double)r * pi_l / (long double)(kSinTable / 2);
-        const double s0 = (double)sinl(ang), c0 = (double)cosl(ang);
-        const double sv[4] = {s0, c0, -s0, -c0}, cv[4] = {c0, -s0, -c0, s0};
-        tab[(size_t)k] = make_double2(sv[q], cv[q]);
-      }
+      const std::vector<longlong2> tab = build_sin_table();
       p->t.sincos = p->up(tab.data(), tab.size());
     }
     // factor blocks (column-major copy for the forward pass, row-major for the backward pass)
@@ -1908,6 +2047,19 @@ int jja_eval_sin(jja_plan* p, const double* x, double* out, int64_t n, void* str
     k_eval_sin<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(x, out, n, p->t.sincos);
     g_launches++;
     JJA_CUDA(cudaGetLastError());
+  });
+}
+
+int jja_sin_host(const double* x, double* s, double* c, int64_t n) {
+  return guarded([&] {
+    if (!x || n < 0 || (!s && !c)) throw Error(JJA_ERR_ARG, "jja_sin_host: bad arguments");
+    static const std::vector<longlong2> tab = build_sin_table();
+    for (int64_t i = 0; i < n; ++i) {
+      double sv, cv;
+      fast_sincos(x[i], tab.data(), sv, cv);
+      if (s) s[i] = c ? sv : fast_sin(x[i], tab.data());
+      if (c) c[i] = cv;
+    }
   });
 }
 

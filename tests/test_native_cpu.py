@@ -85,6 +85,32 @@ def test_nested_dissection_fill_is_bounded():
     assert st["n_levels"] <= 30
 
 
+def test_fixed_point_sine_on_host():
+    """The junction kernels' sine and cosine (64-bit fixed point + FP32, no FP64 instruction),
+    run on the host from the same source: within 1.2e-16 absolute of numpy for |x| < 2^62; near
+    zeros of sine within 1e-18 absolute (a few units of the fixed point's 2^-62) plus 2 ulps;
+    x itself below 2^-27; NaN from 2^62 on and for inf and NaN."""
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(-1e4, 1e4, 400000), rng.uniform(-4, 4, 200000),
+                        np.arange(-3000, 3000) * (np.pi / 2048) + rng.uniform(-1e-9, 1e-9, 6000),
+                        np.arange(-3000, 3000) * (np.pi / 2) + rng.uniform(-1e-7, 1e-7, 6000),
+                        10.0 ** rng.uniform(-12, 18.6, 300000), rng.uniform(-2e5, 2e5, 100000),
+                        np.array([0.0, -0.0, 1e-300, 2.0 ** -27, -(2.0 ** -27), np.pi, 1e5, 199999.99, 2e5, 3e5,
+                                  -7e6, 2.0 ** 62 * (1 - 2.0 ** -53), 2.0 ** 62, -1e300, np.inf, -np.inf, np.nan])])
+    s, c = np.empty_like(x), np.empty_like(x)
+    N.check(N.lib().jja_sin_host(N.ptr(x), N.ptr(s), N.ptr(c), x.size))
+    with np.errstate(invalid="ignore"):
+        rs, rc = np.sin(x), np.cos(x)
+    fin = np.abs(x) < 2.0 ** 62     # beyond, and for inf and NaN: NaN
+    assert np.all(np.isnan(s[~fin])) and np.all(np.isnan(c[~fin]))
+    assert np.abs(s - rs)[fin].max() <= 1.2e-16 and np.abs(c - rc)[fin].max() <= 1.2e-16
+    tiny = np.abs(x) < 2.0 ** -27
+    assert np.array_equal(s[tiny], x[tiny]) and np.all(c[tiny] == 1.0)
+    xf = np.where(fin, x, 0.0)
+    near = fin & (np.abs(xf - np.round(xf / np.pi) * np.pi) < np.pi / 4096) & (np.abs(xf) < 2e5)
+    assert near.sum() > 1000 and np.all(np.abs(s - rs)[near] <= 1e-18 + 2.3e-16 * np.abs(rs[near]))
+
+
 def test_auto_ordering_policy():
     # minimum degree only where the step is FP64-bound (lots of face-problems) and SuperLU's
     # host ordering run stays cheap; explicit orderings pass through
