@@ -43,6 +43,13 @@ def _compact(v):
     return v[:1 if v.strides[0] == 0 else v.shape[0], :1 if v.strides[1] == 0 else v.shape[1]]
 
 
+def _host_f64(a):
+    """A C-contiguous, writable float64 array with a's values: a itself when it already is one
+    (no copy of the large inputs), else a copy (torch.from_numpy needs writable memory)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a if a.flags.writeable else a.copy()
+
+
 def _source_is_zero(timedep, getter, N_rows, W):
     """The reference's zero test ``np.allclose(x, 0)`` for time-independent sources
     (time_evolution.py:512-519), evaluated on the non-broadcast part: |x| <= 1e-8 everywhere
@@ -82,7 +89,7 @@ class _Source:
             self.shape = (rows, cols)
             self.buf = torch.empty(self.shape, dtype=torch.float64, device=dev)
             self.view = N.View(self.buf.data_ptr(), cols if rows > 1 else 0, 1 if cols > 1 else 0, 0)
-            host = np.array(v0[:rows, :cols], dtype=np.float64, order="C")
+            host = _host_f64(v0[:rows, :cols])
             with torch.cuda.stream(stream):
                 self.buf.copy_(torch.from_numpy(host))
             self.h2d_bytes += host.nbytes
@@ -194,7 +201,7 @@ class GpuSimulation:
             self.hist = []
             with torch.cuda.stream(self.stream):
                 for h in hist0:
-                    h = np.array(np.broadcast_to(h, (self.Nj, self.W)), np.float64, order="C")
+                    h = _host_f64(h if np.shape(h) == (self.Nj, self.W) else np.broadcast_to(h, (self.Nj, self.W)))
                     zero = not np.any(h)
                     self.hist0_zero.append(zero)
                     if zero:      # the default initial condition: no host->device copy needed

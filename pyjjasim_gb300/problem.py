@@ -62,7 +62,7 @@ class TimeEvolutionProblem:
         self.current_phase_relation = DefaultCPR() if current_phase_relation is None else current_phase_relation
 
         def count(x):
-            s = np.array(x(0) if callable(x) else x).shape
+            s = np.shape(x(0) if callable(x) else x)
             return s[1] if len(s) > 1 else 1
 
         self.problem_count = max(count(external_flux), count(current_sources), count(voltage_sources),
@@ -173,7 +173,7 @@ class TimeEvolutionProblem:
     def _is_timedep(x):
         if callable(x):
             return True
-        s = np.array(x).shape
+        s = np.shape(x)
         return len(s) > 0 and s[-1] > 1
 
     def _step_value(self, x, N, i):
@@ -213,10 +213,17 @@ class TimeEvolutionProblem:
 def _stencil_derivative(x_tm, index, s1, dt):
     """Backward-stencil derivative at stored slots ``index`` of a time-major (slots, Nj, W)
     array, returned time-major (time_evolution.py:411-420, same operation order)."""
-    out = s1[0] * x_tm[index]
+    out = x_tm[index]          # a copy (integer-array index)
+    if s1[0] != 1.0:           # 1 x is exact: skip the pass
+        out *= s1[0]
     for k in range(1, len(s1) - 1):
-        out = out + s1[k] * x_tm[index - k]
-    return out / dt
+        for j, i in enumerate(index):   # slot by slot: no temporary of all slots
+            if s1[k] == -1.0:           # -1 x then add: the same rounding as a subtraction
+                np.subtract(out[j], x_tm[i - k], out=out[j])
+            else:
+                out[j] += s1[k] * x_tm[i - k]
+    out /= dt
+    return out
 
 
 def _select_slots(x, slots):
@@ -331,11 +338,12 @@ class TimeEvolutionResult:
         return self.current[:, :, self._time_point_index(tp)]
 
     def _select(self, select_time_points, N, func):
+        # filled time-major (contiguous copies) and returned as the (N, W, T) view
         sel = np.flatnonzero(self.problem._to_time_point_mask(select_time_points))
-        out = np.zeros((N, self.get_problem_count(), len(sel)), dtype=np.double)
+        out = np.empty((len(sel), N, self.get_problem_count()), dtype=np.double)
         for k, tp in enumerate(sel):
-            out[:, :, k] = func(tp)
-        return out
+            out[k] = func(tp)
+        return out.transpose(1, 2, 0)
 
     def get_theta(self, select_time_points=None):
         return self._select(select_time_points, self.get_circuit()._Nj(), self._th)
