@@ -99,6 +99,10 @@ typedef struct {
   int pdl;            /* 1: launch the step's kernels with programmatic dependent launch (each
                          launch overlaps the tail of the kernel before; measured: 6 % faster for
                          W = 1, 5-7 % slower for W >= 64); 0: default (plain launches) */
+  int groups;         /* level schedule: step the problems as this many independent groups, each
+                         on its own stream (created by the plan; the call's stream forks to them
+                         and joins back before jja_run returns), so their launch chains overlap;
+                         0: default (W / 160 clamped to [2, 4] from W = 256 on, else 1) */
 } jja_solve_tuning;
 
 /* Builds on the host (no GPU needed) the work-item schedule that jja_plan_create would make for

@@ -8,7 +8,10 @@ GPU depends on choices that have no single best value across array sizes and bat
 * ``pdl``: programmatic dependent launch of the step's kernels (launch latency hidden behind
   the previous kernel's tail; pays off when the kernels are short);
 * ``ordering``: nested dissection (shallow tree, big supernodes) or minimum degree (about 30 %
-  less fill on 2-D arrays, but a deeper tree of smaller supernodes);
+  less fill on 2-D arrays, but a deeper tree of smaller supernodes); ``"auto"`` (the library's
+  default) picks by the step's size;
+* ``groups``: the step's problems as independent groups on concurrent streams (each fills the
+  SMs the other groups' level tails leave idle);
 * ``relax``: how far supernodes are amalgamated (fewer, wider supernodes and fewer elimination-
   tree levels, i.e. fewer launches, against extra flops on explicit zeros);
 * ``rows_per_lane`` (1, 2, 4, 8): output rows a lane accumulates per work item (more FMAs per load
@@ -34,13 +37,14 @@ import numpy as np
 from . import plan as P
 
 CACHE_ENV = "PYJJASIM_GB300_TUNE_CACHE"
-DEFAULT = {"schedule": 1, "ordering": "nd", "relax": (-1, -1.0), "rows_per_lane": 0, "rows_per_lane_fwd": 0,
-           "rhs_block": 0, "target_warps": 152 * 24, "pdl": 0}
+DEFAULT = {"schedule": 1, "ordering": "auto", "relax": (-1, -1.0), "rows_per_lane": 0, "rows_per_lane_fwd": 0,
+           "rhs_block": 0, "target_warps": 152 * 24, "pdl": 0, "groups": 0}
 # searched in this order; a tuple is searched jointly (ordering and rows per lane interact:
 # minimum degree's smaller supernodes want fewer rows per warp). Rows per lane 0 = the library's
 # defaults (1, and 2 in the forward sweep from W = 256 on); a nonzero value sets both sweeps
 # unless rows_per_lane_fwd sets the forward one.
-AXES = (("ordering", "rows_per_lane"), "rows_per_lane_fwd", "schedule", "pdl", "rhs_block", "target_warps", "relax")
+AXES = (("ordering", "rows_per_lane"), "rows_per_lane_fwd", "schedule", "pdl", "groups", "rhs_block", "target_warps",
+        "relax")
 
 
 def cache_path():
@@ -61,7 +65,8 @@ def candidates(W):
     return {
         "schedule": [1, 2],
         "pdl": [0, 1],
-        "ordering": ["nd", "mmd"],
+        "ordering": ["auto", "nd", "mmd"],
+        "groups": [0, 1, 2, 3, 4] if W >= 64 else [0],
         "rows_per_lane": [0, 1, 2, 4],
         "rows_per_lane_fwd": [0, 1, 2, 4],
         "rhs_block": [0] + [b for b in (wb // 2, wb // 4) if b >= 1],
@@ -76,7 +81,8 @@ def to_options(cfg):
             "tuning": {"rows_per_lane": int(cfg["rows_per_lane"]),
                        "rows_per_lane_fwd": int(cfg.get("rows_per_lane_fwd", 0)),
                        "rhs_block": int(cfg["rhs_block"]), "target_warps": int(cfg["target_warps"]),
-                       "schedule": int(cfg["schedule"]), "pdl": int(cfg.get("pdl", 0))}}
+                       "schedule": int(cfg["schedule"]), "pdl": int(cfg.get("pdl", 0)),
+                       "groups": int(cfg.get("groups", 0))}}
 
 
 def coordinate_descent(W, measure, min_gain=0.02):

@@ -73,6 +73,8 @@ constexpr int kDefaultRowsPerLaneFwdWide = 2;   // the forward sweep's default f
 constexpr int kDefaultPackRows = 24;   // W = 1: supernodes of at most this many rows go one per lane
 constexpr int kPackMaxK = 8;           // ... and at most this many columns
 constexpr int kDefaultPackMinWarps = 152 * 64 * 2;   // ... on levels with at least two waves of warps
+constexpr int kGroupsFromW = 256;      // from this many problems the step runs as concurrent groups ...
+constexpr int kGroupW = 160;           // ... of about this many problems, 2 to 4 of them
 constexpr int kDefaultTargetWarps = 152 * 24;   // levels with fewer work items split their dot products
 constexpr int kDefaultMinPiece = 16;     // shortest piece of a split dot product
 constexpr int kUnroll = JJA_UNROLL;   // columns whose loads are issued ahead of their FMAs
@@ -123,6 +125,7 @@ __device__ __forceinline__ double view_at(const jja_view& v, int64_t n, int64_t 
 
 struct StepArgs {
   int Nj, Nf, W, width;
+  int w0, wn;          // the launch steps problems [w0, w0 + wn) of the W in the arrays (a group)
   const double* h[4];
   double* hout;
   double* theta_s;
@@ -417,10 +420,10 @@ __global__ void __launch_bounds__(256) k_scale_sources(jja_view Is, const double
 // q for the first step of a run, from the stored phase history
 __global__ void __launch_bounds__(256) k_junction(StepArgs a, Tables t, double* __restrict__ q) {
   pdl_begin();
-  const int64_t NjW = (int64_t)a.Nj * a.W;
+  const int64_t n = (int64_t)a.Nj * a.wn;
   const int64_t step = a.d_step[0], tt = step - a.d_step[2];
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t j = e / a.W, w = e - j * a.W;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = i / a.wn, w = a.w0 + (i - j * a.wn), e = j * a.W + w;
     double th[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) th[k] = (k < a.width - 1) ? a.h[k][e] : 0.0;
@@ -443,10 +446,10 @@ __global__ void k_set_counters(int64_t* __restrict__ d_step, int64_t step, int64
 __global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const double* __restrict__ q,
                                                   double* __restrict__ b) {
   pdl_begin();
-  const int64_t NfW = (int64_t)a.Nf * a.W;
+  const int64_t n = (int64_t)a.Nf * a.wn;
   const int64_t step = a.d_step[0], tt = step - a.d_step[2];
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NfW; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t p = e / a.W, w = e - p * a.W;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = i / a.wn, w = a.w0 + (i - p * a.wn), e = p * a.W + w;
     double acc = 0.0;
     if (t.face_deg) {
       // fixed-degree layout: all index loads, then all value loads, then the sum
@@ -466,13 +469,13 @@ __global__ void __launch_bounds__(256) k_face_rhs(StepArgs a, Tables t, const do
         if (code[d] >= 0) acc += signed_by(v[d], code[d] & 1);
     } else {
       const int64_t i0 = __ldg(t.fj_ptr + p), i1 = __ldg(t.fj_ptr + p + 1);
-      for (int64_t i = i0; i < i1; ++i) {
-        const int code = __ldg(t.fj_col + i);          // (junction << 1) | (A entry is -1)
+      for (int64_t k = i0; k < i1; ++k) {
+        const int code = __ldg(t.fj_col + k);          // (junction << 1) | (A entry is -1)
         const int64_t j = code >> 1;
         double v = q[j * a.W + w];
         if (a.theta_s) v -= a.theta_s[j * a.W + w];
         v = signed_by(v, code & 1);
-        acc = (i == i0) ? v : acc + v;
+        acc = (k == i0) ? v : acc + v;
       }
     }
     if (a.f.ptr) acc = fma(-kTwoPi, view_at(a.f, __ldg(t.face_orig + p), w, tt), acc);
@@ -491,11 +494,11 @@ template <bool kFuseNext>
 __global__ void __launch_bounds__(256, JJA_UPDATE_MIN_BLOCKS) k_update(StepArgs a, Tables t, double* __restrict__ q,
                                                 const double* __restrict__ J) {
   pdl_begin();
-  const int64_t NjW = (int64_t)a.Nj * a.W;
+  const int64_t NjW = (int64_t)a.Nj * a.W, n = (int64_t)a.Nj * a.wn;
   const int64_t next_step = a.d_step[1];            // published by this step's k_face_rhs
   const int64_t tt = next_step - 1 - a.d_step[2];   // source slot of the step being finished
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < NjW; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t j = e / a.W, w = e - j * a.W;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = i / a.wn, w = a.w0 + (i - j * a.wn), e = j * a.W + w;
     // y = A^T J: a junction lies on one or two faces; the +-1 entries are sign flips
     const int p0 = __ldg(t.jf_face + 2 * j), p1 = __ldg(t.jf_face + 2 * j + 1);
     double y = p0 >= 0 ? signed_by(J[(int64_t)(p0 >> 1) * a.W + w], p0 & 1) : 0.0;
@@ -545,15 +548,15 @@ __device__ __forceinline__ Item unpack_item(int4 v) {
   return it;
 }
 
-// zero the listed rows of an (Nf x W) vector before a sweep whose partial items accumulate
+// zero the listed rows (columns [w0, w0 + wn)) of an (Nf x W) vector before a sweep whose partial items accumulate
 // there, and the sweep's dataflow counters (n_ctr of them, none for level-synchronous sweeps)
-__global__ void k_zero_rows(double* __restrict__ v, const int32_t* __restrict__ rows, int n_rows, int W,
-                            unsigned* __restrict__ ctr, int n_ctr) {
+__global__ void k_zero_rows(double* __restrict__ v, const int32_t* __restrict__ rows, int n_rows, int W, int w0,
+                            int wn, unsigned* __restrict__ ctr, int n_ctr) {
   pdl_begin();
-  const int64_t n = (int64_t)n_rows * W;
+  const int64_t n = (int64_t)n_rows * wn;
   const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
   for (int64_t e = tid; e < n; e += nth) {
-    const int64_t i = e / W, w = e - i * W;
+    const int64_t i = e / wn, w = w0 + (e - i * wn);
     v[(int64_t)__ldg(rows + i) * W + w] = 0.0;
   }
   for (int64_t e = tid; e < n_ctr; e += nth) ctr[e] = 0u;
@@ -1075,7 +1078,8 @@ void for_each_supernode(const Schedule& S, const int4& v, Fn fn) {
   for (int l = 0; l < v.y; ++l) fn(S.pack_sn[first + l]);
 }
 
-Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu) {
+// the work items of problems [w_lo, w_hi) (w_hi < 0: all W); w_lo a multiple of the RHS block
+Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu, int w_lo = 0, int w_hi = -1) {
   if (W <= 0 || W >= (1 << 30)) throw Error(JJA_ERR_ARG, "W must be in [1, 2^30)");
   for (int v : {tu.rows_per_lane, tu.rows_per_lane_fwd})
     if (v && v != 1 && v != 2 && v != 4 && v != 8)
@@ -1085,7 +1089,10 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu)
   if (tu.pdl < 0 || tu.pdl > 1) throw Error(JJA_ERR_ARG, "pdl must be 0 or 1");
   if (tu.pack_rows > 256) throw Error(JJA_ERR_ARG, "pack_rows must be <= 256");
   if (tu.pack_min_warps < 0) throw Error(JJA_ERR_ARG, "pack_min_warps must be >= 0");
+  if (tu.groups < 0 || tu.groups > 64) throw Error(JJA_ERR_ARG, "groups must be in [0, 64]");
   const int WB = resolve_rhs_block(W, tu);
+  if (w_hi < 0) w_hi = W;
+  if (w_lo < 0 || w_lo >= w_hi || w_hi > W || w_lo % WB) throw Error(JJA_ERR_INTERNAL, "bad problem range");
   // W = 1 packs of small supernodes (level schedule only: the dataflow sweep counts items per
   // supernode)
   const int pack_rows = (W == 1 && tu.schedule != 2 && tu.pack_rows >= 0)
@@ -1109,7 +1116,7 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu)
   };
   // Levels with fewer items than can fill the GPU split each dot product into pieces of at
   // least min_piece terms (multiples of the unroll), enough to reach target_warps warps.
-  const int nwc = (W + WB - 1) / WB;
+  const int nwc = (w_hi - w_lo + WB - 1) / WB;
   auto pieces_of = [&](int len, int split) {
     const int np = std::max(1, std::min(split, len / min_piece));
     const int plen = ((len + np - 1) / np + kUnroll - 1) / kUnroll * kUnroll;
@@ -1141,7 +1148,7 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu)
         const bool partial = jmax > fplen;
         zf_s |= partial && r0 < k;
         for (int c_lo = 0; c_lo < jmax; c_lo += fplen)
-          for (int w0 = 0; w0 < W; w0 += WB)
+          for (int w0 = w_lo; w0 < w_hi; w0 += WB)
             S.fi.push_back(pack(s, r0, r1, w0, partial, c_lo, std::min(jmax, c_lo + fplen)));
       }
       for (int i0 = 0; i0 < k; i0 += RPI_b) {
@@ -1150,7 +1157,7 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu)
         const bool partial = len > bplen;
         zb_s |= partial;
         for (int c_lo = i0; c_lo < nf; c_lo += bplen)
-          for (int w0 = 0; w0 < W; w0 += WB)
+          for (int w0 = w_lo; w0 < w_hi; w0 += WB)
             S.bi.push_back(pack(s, i0, i1, w0, partial, c_lo, std::min(nf, c_lo + bplen)));
       }
       if (zf_s) for (int i = 0; i < k; ++i) S.zf.push_back(c0 + i);
@@ -1280,6 +1287,26 @@ struct jja_factor {
   std::unique_ptr<jja::Factor> f;
 };
 
+// Problems [w0, w0 + wn) stepped as one chain of launches: their work items per level, the rows
+// that split dot products accumulate into, their step counters, and their stream (null: the
+// caller's). A plan holds the group of all its problems (used by solves, the adjoint and the
+// dataflow schedule) and, when it steps its problems in independent groups, those: the groups'
+// chains run concurrently, so each fills the SMs the other's level tails and latency-bound
+// launches leave idle.
+struct Group {
+  int w0 = 0, wn = 0;
+  std::vector<int64_t> fwd_ptr, bwd_ptr;
+  std::vector<char> level_packed;
+  int4* fwd_items = nullptr;
+  int4* bwd_items = nullptr;        // levels ascending (level launches index them per level)
+  int32_t* zrows_f = nullptr;       // rows of z accumulated by partial forward items
+  int32_t* zrows_b = nullptr;       // rows of x accumulated by partial backward items
+  int nz_f = 0, nz_b = 0;
+  int64_t* d_step = nullptr;        // step counters (see StepArgs)
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;       // end of the group's chain in a call (joined by the caller's stream)
+};
+
 struct jja_plan {
   int Nj = 0, Nf = 0, W = 0, width = 3, WB = 1, n_levels = 0;
   int rows_per_lane = kDefaultRowsPerLane, rows_per_lane_fwd = kDefaultRowsPerLane;   // backward, forward
@@ -1288,19 +1315,14 @@ struct jja_plan {
   Tables t{};
   FactorDev F{};
   std::vector<void*> allocs;
-  std::vector<int64_t> fwd_ptr, bwd_ptr;
-  std::vector<char> level_packed;
-  int4* fwd_items = nullptr;
-  int4* bwd_items = nullptr;        // levels ascending (level launches index them per level)
-  int4* bwd_flow_items = nullptr;   // the same items root first (dataflow sweep order)
+  Group all;                        // all W problems
+  std::vector<Group> groups;        // the step's independent groups (empty: one, `all`)
+  cudaEvent_t fork = nullptr;       // start of a call on the caller's stream (the groups wait on it)
+  int4* bwd_flow_items = nullptr;   // the backward items of `all` root first (dataflow sweep order)
   double *b = nullptr, *z = nullptr, *x = nullptr, *xj = nullptr;
   int32_t* perm = nullptr;   // new -> old face
-  int64_t* d_step = nullptr;
   double* isq = nullptr;        // Is / c0 (Nj x W)
   int resistive = 0;
-  int32_t* zrows_f = nullptr;   // rows of z accumulated by partial forward items
-  int32_t* zrows_b = nullptr;   // rows of x accumulated by partial backward items
-  int nz_f = 0, nz_b = 0;
   // dataflow sweeps (schedule 2): dependency tables per supernode, counters, error flag
   int flow = 0, ns = 0;
   const int32_t* f_wait_on = nullptr;
@@ -1325,6 +1347,11 @@ struct jja_plan {
   ~jja_plan() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
     for (auto& g : adj_graphs) cudaGraphExecDestroy(g.exec);
+    for (Group& g : groups) {
+      if (g.stream) cudaStreamDestroy(g.stream);
+      if (g.done) cudaEventDestroy(g.done);
+    }
+    if (fork) cudaEventDestroy(fork);
     for (void* p : allocs) cudaFree(p);
   }
   template <class T>
@@ -1361,15 +1388,18 @@ void launch(bool pdl, void (*kernel)(KArgs...), int grid, int block, cudaStream_
 
 // zero the rows that partial items of the coming sweep accumulate into (and, for a dataflow
 // sweep, its counters)
-void launch_zero_rows(jja_plan* p, cudaStream_t st, bool forward, double* v) {
-  const int n = forward ? p->nz_f : p->nz_b;
+void launch_zero_rows(jja_plan* p, const Group& g, cudaStream_t st, bool forward, double* v) {
+  const int n = forward ? g.nz_f : g.nz_b;
   const int n_ctr = p->flow ? p->ns + 1 : 0;
   if (!n && !n_ctr) return;
   unsigned* ctr = p->flow ? p->counters + (forward ? 0 : p->ns + 1) : nullptr;
-  launch(p->pdl, k_zero_rows, grid_for(std::max<int64_t>((int64_t)n * p->W, n_ctr), 256), 256, st, v,
-         (const int32_t*)(forward ? p->zrows_f : p->zrows_b), n, p->W, ctr, n_ctr);
+  launch(p->pdl, k_zero_rows, grid_for(std::max<int64_t>((int64_t)n * g.wn, n_ctr), 256), 256, st, v,
+         (const int32_t*)(forward ? g.zrows_f : g.zrows_b), n, p->W, g.w0, g.wn, ctr, n_ctr);
 }
 
+void launch_zero_rows(jja_plan* p, cudaStream_t st, bool forward, double* v) { launch_zero_rows(p, p->all, st, forward, v); }
+
+// the dataflow sweep: all problems in one persistent launch (the schedule of `all`)
 template <int RPL>
 void launch_flow(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x,
                  const uint32_t* wait_count_override = nullptr) {
@@ -1382,88 +1412,97 @@ void launch_flow(jja_plan* p, cudaStream_t st, bool forward, double* b, double* 
   fl.wait_count = wait_count_override ? wait_count_override : (forward ? p->f_wait_count : p->b_wait_count);
   fl.notify = forward ? p->f_notify : p->b_notify;
   fl.err = p->flow_err;
-  const int n = (int)(forward ? p->fwd_ptr.back() : p->bwd_ptr.back());
+  const int n = (int)(forward ? p->all.fwd_ptr.back() : p->all.bwd_ptr.back());
   if (!n) return;
   const int grid = std::max(1, std::min((n + kWarpsPerBlock - 1) / kWarpsPerBlock, p->flow_blocks[vi][forward]));
   if (forward)
-    launch(p->pdl, k_flow_sweep<RPL, true>, grid, kWarpsPerBlock * 32, st, p->F, (const int4*)p->fwd_items, n, p->W,
-           p->WB, b, z, x, fl);
+    launch(p->pdl, k_flow_sweep<RPL, true>, grid, kWarpsPerBlock * 32, st, p->F, (const int4*)p->all.fwd_items, n,
+           p->W, p->WB, b, z, x, fl);
   else
     launch(p->pdl, k_flow_sweep<RPL, false>, grid, kWarpsPerBlock * 32, st, p->F, (const int4*)p->bwd_flow_items, n,
            p->W, p->WB, b, z, x, fl);
 }
 
 template <int RPL>
-void launch_sweep(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x) {
+void launch_sweep(jja_plan* p, const Group& g, cudaStream_t st, bool forward, double* b, double* z, double* x) {
   if (p->flow) {
     launch_flow<RPL>(p, st, forward, b, z, x);
     return;
   }
   if (forward) {  // levels ascending (children before parents); b is consumed, z produced
     for (int l = 0; l < p->n_levels; ++l) {
-      const int n = (int)(p->fwd_ptr[l + 1] - p->fwd_ptr[l]);
+      const int n = (int)(g.fwd_ptr[l + 1] - g.fwd_ptr[l]);
       if (!n) continue;
-      launch(p->pdl, p->level_packed[l] ? k_fwd_level<RPL, true> : k_fwd_level<RPL, false>,
+      launch(p->pdl, g.level_packed[l] ? k_fwd_level<RPL, true> : k_fwd_level<RPL, false>,
              (n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, st, p->F,
-             (const int4*)(p->fwd_items + p->fwd_ptr[l]), n, p->W, p->WB, b, z);
+             (const int4*)(g.fwd_items + g.fwd_ptr[l]), n, p->W, p->WB, b, z);
     }
   } else {        // levels descending; x produced
     for (int l = p->n_levels - 1; l >= 0; --l) {
-      const int n = (int)(p->bwd_ptr[l + 1] - p->bwd_ptr[l]);
+      const int n = (int)(g.bwd_ptr[l + 1] - g.bwd_ptr[l]);
       if (!n) continue;
-      launch(p->pdl, p->level_packed[l] ? k_bwd_level<RPL, true> : k_bwd_level<RPL, false>,
+      launch(p->pdl, g.level_packed[l] ? k_bwd_level<RPL, true> : k_bwd_level<RPL, false>,
              (n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, st, p->F,
-             (const int4*)(p->bwd_items + p->bwd_ptr[l]), n, p->W, p->WB, (const double*)z, x);
+             (const int4*)(g.bwd_items + g.bwd_ptr[l]), n, p->W, p->WB, (const double*)z, x);
     }
   }
 }
 
 // one triangular sweep over the levels with the plan's rows-per-lane variant of the kernels
-void launch_sweep_any(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x) {
+void launch_sweep_any(jja_plan* p, const Group& g, cudaStream_t st, bool forward, double* b, double* z, double* x) {
   switch (forward ? p->rows_per_lane_fwd : p->rows_per_lane) {
-    case 1: launch_sweep<1>(p, st, forward, b, z, x); break;
-    case 2: launch_sweep<2>(p, st, forward, b, z, x); break;
-    case 8: launch_sweep<8>(p, st, forward, b, z, x); break;
-    default: launch_sweep<4>(p, st, forward, b, z, x); break;
+    case 1: launch_sweep<1>(p, g, st, forward, b, z, x); break;
+    case 2: launch_sweep<2>(p, g, st, forward, b, z, x); break;
+    case 8: launch_sweep<8>(p, g, st, forward, b, z, x); break;
+    default: launch_sweep<4>(p, g, st, forward, b, z, x); break;
   }
 }
 
-void launch_levels(jja_plan* p, cudaStream_t st, bool forward) {
-  launch_zero_rows(p, st, forward, forward ? p->z : p->x);
-  launch_sweep_any(p, st, forward, p->b, p->z, p->x);
+void launch_sweep_any(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x) {
+  launch_sweep_any(p, p->all, st, forward, b, z, x);
 }
 
-// q of the first step of a run, from the phase history
+void launch_levels(jja_plan* p, const Group& g, cudaStream_t st, bool forward) {
+  launch_zero_rows(p, g, st, forward, forward ? p->z : p->x);
+  launch_sweep_any(p, g, st, forward, p->b, p->z, p->x);
+}
+
+void launch_levels(jja_plan* p, cudaStream_t st, bool forward) { launch_levels(p, p->all, st, forward); }
+
+// q of the first step of a run, from the phase history (the args' group of problems)
 void launch_junction(jja_plan* p, StepArgs& a, cudaStream_t st) {
-  launch(p->pdl, k_junction, grid_for((int64_t)p->Nj * p->W, 256), 256, st, a, p->t, p->xj);
+  launch(p->pdl, k_junction, grid_for((int64_t)p->Nj * a.wn, 256), 256, st, a, p->t, p->xj);
 }
 
-// one time step whose q is already in p->xj; `fuse_next` also leaves the next step's q there.
-// With `ev` (5 events) the boundaries face rhs | forward | backward | update(+next q) are recorded.
-void launch_step(jja_plan* p, StepArgs& a, cudaStream_t st, bool fuse_next, cudaEvent_t* ev = nullptr) {
-  const int64_t NjW = (int64_t)p->Nj * p->W, NfW = (int64_t)p->Nf * p->W;
+// one time step of group g whose q is already in p->xj; `fuse_next` also leaves the next step's
+// q there. With `ev` (5 events) the boundaries face rhs | forward | backward | update(+next q)
+// are recorded.
+void launch_step(jja_plan* p, const Group& g, StepArgs& a, cudaStream_t st, bool fuse_next,
+                 cudaEvent_t* ev = nullptr) {
+  const int64_t nj = (int64_t)p->Nj * g.wn, nf = (int64_t)p->Nf * g.wn;
   if (ev) JJA_CUDA(cudaEventRecord(ev[0], st));
-  launch(p->pdl, k_face_rhs, grid_for(NfW, 256), 256, st, a, p->t, (const double*)p->xj, p->b);
+  launch(p->pdl, k_face_rhs, grid_for(nf, 256), 256, st, a, p->t, (const double*)p->xj, p->b);
   if (ev) JJA_CUDA(cudaEventRecord(ev[1], st));
-  launch_levels(p, st, true);
+  launch_levels(p, g, st, true);
   if (ev) JJA_CUDA(cudaEventRecord(ev[2], st));
-  launch_levels(p, st, false);
+  launch_levels(p, g, st, false);
   if (ev) JJA_CUDA(cudaEventRecord(ev[3], st));
-  if (fuse_next) launch(p->pdl, k_update<true>, grid_for(NjW, 256), 256, st, a, p->t, p->xj, (const double*)p->x);
-  else launch(p->pdl, k_update<false>, grid_for(NjW, 256), 256, st, a, p->t, p->xj, (const double*)p->x);
+  if (fuse_next) launch(p->pdl, k_update<true>, grid_for(nj, 256), 256, st, a, p->t, p->xj, (const double*)p->x);
+  else launch(p->pdl, k_update<false>, grid_for(nj, 256), 256, st, a, p->t, p->xj, (const double*)p->x);
   if (ev) JJA_CUDA(cudaEventRecord(ev[4], st));
 }
 
-StepArgs make_args(jja_plan* p, jja_state* s) {
+StepArgs make_args(jja_plan* p, jja_state* s, const Group& g) {
   StepArgs a{};
   a.Nj = p->Nj; a.Nf = p->Nf; a.W = p->W; a.width = p->width;
+  a.w0 = g.w0; a.wn = g.wn;
   for (int k = 0; k < 4; ++k) { a.h[k] = s->hist[k]; a.e[k] = p->extrap[k]; }
   a.theta_s = s->theta_s;
   a.Is = s->Is; a.f = s->f; a.Vs = s->Vs; a.T = s->T;
   a.noise_mode = s->noise_mode;
   a.noise = s->noise;
   a.seed = s->seed;
-  a.d_step = p->d_step;
+  a.d_step = g.d_step;
   a.th_out = s->th_out;
   a.I_out = s->I_out;
   a.store_all = s->store_all ? 1 : 0;
@@ -1500,11 +1539,42 @@ void check_window(const jja_state* s, int nsteps, const char* who) {
   }
 }
 
-void set_counters(jja_plan* p, const jja_state* s, cudaStream_t st) {
-  launch(p->pdl, k_set_counters, 1, 1, st, p->d_step, s->step, s->src_t0);
+// the groups a call steps: the plan's independent groups, or the group of all problems
+std::vector<Group*> step_groups(jja_plan* p) {
+  std::vector<Group*> gs;
+  if (p->groups.empty()) gs.push_back(&p->all);
+  for (Group& g : p->groups) gs.push_back(&g);
+  return gs;
 }
 
-// graph of G fused steps for the state's current buffers (captured on first use, then cached)
+// the stream group g runs on in a call on the caller's stream st
+cudaStream_t stream_of(const Group& g, cudaStream_t st) { return g.stream ? g.stream : st; }
+
+// fork: the groups' own streams wait for the caller's stream; join: the caller's stream waits
+// for them. Every call joins before it returns, so work the caller queues next is ordered after
+// all groups.
+void fork_groups(jja_plan* p, cudaStream_t st) {
+  if (p->groups.size() < 2) return;
+  JJA_CUDA(cudaEventRecord(p->fork, st));
+  for (Group& g : p->groups)
+    if (g.stream) JJA_CUDA(cudaStreamWaitEvent(g.stream, p->fork, 0));
+}
+
+void join_groups(jja_plan* p, cudaStream_t st) {
+  if (p->groups.size() < 2) return;
+  for (Group& g : p->groups) {
+    if (!g.stream) continue;
+    JJA_CUDA(cudaEventRecord(g.done, g.stream));
+    JJA_CUDA(cudaStreamWaitEvent(st, g.done, 0));
+  }
+}
+
+void set_counters(jja_plan* p, const jja_state* s, cudaStream_t st) {
+  for (Group* g : step_groups(p)) launch(p->pdl, k_set_counters, 1, 1, st, g->d_step, s->step, s->src_t0);
+}
+
+// graph of G fused steps for the state's current buffers (captured on first use, then cached);
+// with several groups the graph forks into their streams and joins back
 cudaGraphExec_t graph_for(jja_plan* p, const jja_state* s, cudaStream_t st, int G) {
   std::vector<uint64_t> key = {(uint64_t)s->hist[0], (uint64_t)s->hist[1], (uint64_t)s->hist[2],
                                (uint64_t)s->hist[3], (uint64_t)s->theta_s, (uint64_t)s->noise_mode, s->seed,
@@ -1530,15 +1600,20 @@ cudaGraphExec_t graph_for(jja_plan* p, const jja_state* s, cudaStream_t st, int 
   }
   const int period = p->width - 1;
   cudaGraph_t g;
-  jja_state tmp = *s;
+  const std::vector<Group*> gs = step_groups(p);
   JJA_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  for (int q = 0; q < G; ++q) {
-    StepArgs a = make_args(p, &tmp);
-    a.hout = tmp.hist[period - 1];
-    a.th_slot = a.I_slot = -1;
-    launch_step(p, a, st, true);
-    rotate(&tmp, p->width);
+  fork_groups(p, st);
+  for (Group* grp : gs) {   // each group's chain of G steps (the history rotation is the same for all)
+    jja_state tmp = *s;
+    for (int q = 0; q < G; ++q) {
+      StepArgs a = make_args(p, &tmp, *grp);
+      a.hout = tmp.hist[period - 1];
+      a.th_slot = a.I_slot = -1;
+      launch_step(p, *grp, a, stream_of(*grp, st), true);
+      rotate(&tmp, p->width);
+    }
   }
+  join_groups(p, st);
   JJA_CUDA(cudaStreamEndCapture(st, &g));
   cudaGraphExec_t exec = nullptr;
   const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
@@ -1747,18 +1822,45 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     const Schedule S = build_schedule(F, d->W, tu);
     check_schedule(S);
     p->n_levels = S.n_levels;
-    p->fwd_ptr = S.fwd_ptr;
-    p->bwd_ptr = S.bwd_ptr;
-    p->level_packed = S.level_packed;
-    p->fwd_items = p->up(S.fi.data(), S.fi.size());
-    p->bwd_items = p->up(S.bi.data(), S.bi.size());
+    auto set_group = [&](Group& g, const Schedule& Sg, int w0, int wn) {
+      g.w0 = w0;
+      g.wn = wn;
+      g.fwd_ptr = Sg.fwd_ptr;
+      g.bwd_ptr = Sg.bwd_ptr;
+      g.level_packed = Sg.level_packed;
+      g.fwd_items = p->up(Sg.fi.data(), Sg.fi.size());
+      g.bwd_items = p->up(Sg.bi.data(), Sg.bi.size());
+      g.nz_f = (int)Sg.zf.size();
+      g.nz_b = (int)Sg.zb.size();
+      g.zrows_f = p->up(Sg.zf.data(), Sg.zf.size());
+      g.zrows_b = p->up(Sg.zb.data(), Sg.zb.size());
+      g.d_step = p->up<int64_t>(nullptr, 4);
+      JJA_CUDA(cudaMemset(g.d_step, 0, 4 * sizeof(int64_t)));
+    };
+    set_group(p->all, S, 0, d->W);
     p->bwd_flow_items = p->up(S.bi_flow.data(), S.bi_flow.size());
-  p->F.pack_meta = p->up(S.pack_meta.data(), S.pack_meta.size());
-  p->F.pack_vals = p->up(S.pack_vals.data(), S.pack_vals.size());
-    p->nz_f = (int)S.zf.size();
-    p->nz_b = (int)S.zb.size();
-    p->zrows_f = p->up(S.zf.data(), S.zf.size());
-    p->zrows_b = p->up(S.zb.data(), S.zb.size());
+    p->F.pack_meta = p->up(S.pack_meta.data(), S.pack_meta.size());
+    p->F.pack_vals = p->up(S.pack_vals.data(), S.pack_vals.size());
+    {
+      // independent groups of problems for the step (level schedule only). Measured per step on
+      // 128x128 arrays: W = 256 0.80 -> 0.70 ms with 2 groups; W = 512 1.36 -> 1.26 / 1.23 /
+      // 1.23 ms with 2 / 3 / 4; W = 1024 2.61 -> 2.36 / 2.31 ms with 2 / 4; W = 64 (64x64) no gain
+      const int chunks = (d->W + p->WB - 1) / p->WB;
+      int ng = tu.groups ? tu.groups : (d->W >= kGroupsFromW ? std::max(2, std::min(4, d->W / kGroupW)) : 1);
+      if (tu.schedule == 2) ng = 1;
+      ng = std::max(1, std::min(ng, chunks));
+      if (ng > 1) {
+        p->groups.resize(ng);
+        JJA_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
+        for (int gi = 0; gi < ng; ++gi) {
+          const int lo = (int)((int64_t)chunks * gi / ng) * p->WB;
+          const int hi = std::min(d->W, (int)((int64_t)chunks * (gi + 1) / ng) * p->WB);
+          set_group(p->groups[gi], build_schedule(F, d->W, tu, lo, hi), lo, hi - lo);
+          if (gi > 0) JJA_CUDA(cudaStreamCreateWithFlags(&p->groups[gi].stream, cudaStreamNonBlocking));
+          JJA_CUDA(cudaEventCreateWithFlags(&p->groups[gi].done, cudaEventDisableTiming));
+        }
+      }
+    }
     {
       const int ns = S.ns;
       p->ns = ns;
@@ -1793,8 +1895,6 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->x = p->up<double>(nullptr, NfW);
     p->xj = p->up<double>(nullptr, NjW);
     p->isq = p->up<double>(nullptr, NjW);
-    p->d_step = p->up<int64_t>(nullptr, 4);
-    JJA_CUDA(cudaMemset(p->d_step, 0, 4 * sizeof(int64_t)));
     JJA_CUDA(cudaDeviceSynchronize());
     *out = p.release();
   });
@@ -1919,7 +2019,7 @@ static void launch_adjoint_step(jja_plan* p, const AdjArgs& a, cudaStream_t st) 
   const int64_t NjW = (int64_t)p->Nj * p->W, NfW = (int64_t)p->Nf * p->W;
   k_adj_a<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj);
   StepArgs s{};
-  s.Nj = p->Nj; s.Nf = p->Nf; s.W = p->W; s.width = p->width; s.d_step = p->d_step;
+  s.Nj = p->Nj; s.Nf = p->Nf; s.W = p->W; s.width = p->width; s.w0 = 0; s.wn = p->W; s.d_step = p->all.d_step;
   k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(s, p->t, p->xj, p->b);
   g_launches += 2;
   launch_levels(p, st, true);
@@ -2017,7 +2117,7 @@ int jja_adjoint_flux(jja_plan* p, const double* usum, double* gf, void* stream) 
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t NfW = (int64_t)p->Nf * p->W;
     StepArgs s{};
-    s.Nj = p->Nj; s.Nf = p->Nf; s.W = p->W; s.width = p->width; s.d_step = p->d_step;
+    s.Nj = p->Nj; s.Nf = p->Nf; s.W = p->W; s.width = p->width; s.w0 = 0; s.wn = p->W; s.d_step = p->all.d_step;
     k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(s, p->t, usum, p->b);
     g_launches++;
     launch_levels(p, st, true);
@@ -2075,12 +2175,15 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
     if (nsteps == 0) return;
     check_window(s, nsteps, "jja_run");
     cudaStream_t st = (cudaStream_t)stream;
+    const std::vector<Group*> gs = step_groups(p);
     set_counters(p, s, st);
     launch_scale_sources(p, s, st);
-    {
-      StepArgs a = make_args(p, s);
-      launch_junction(p, a, st);
+    fork_groups(p, st);
+    for (Group* g : gs) {
+      StepArgs a = make_args(p, s, *g);
+      launch_junction(p, a, stream_of(*g, st));
     }
+    join_groups(p, st);
     const int period = p->width - 1;  // history rotation period
     const int G = 16 * period;        // steps per captured graph: pointers return to their places
     int i = 0;
@@ -2101,13 +2204,19 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
         run -= reps * G;
       }
       const int eager = (i < nsteps) ? std::max(run, 1) : 0;
-      for (int q = 0; q < eager && i < nsteps; ++q, ++i) {
-        StepArgs a = make_args(p, s);
-        a.hout = s->hist[period - 1];
-        a.th_slot = th_slot ? th_slot[i] : -1;
-        a.I_slot = I_slot ? I_slot[i] : -1;
-        launch_step(p, a, st, i + 1 < nsteps);
-        rotate(s, p->width);
+      if (eager > 0 && i < nsteps) {
+        fork_groups(p, st);
+        for (int q = 0; q < eager && i < nsteps; ++q, ++i) {
+          for (Group* g : gs) {
+            StepArgs a = make_args(p, s, *g);
+            a.hout = s->hist[period - 1];
+            a.th_slot = th_slot ? th_slot[i] : -1;
+            a.I_slot = I_slot ? I_slot[i] : -1;
+            launch_step(p, *g, a, stream_of(*g, st), i + 1 < nsteps);
+          }
+          rotate(s, p->width);
+        }
+        join_groups(p, st);
       }
     }
     JJA_CUDA(cudaGetLastError());
@@ -2126,16 +2235,39 @@ int jja_run_timed(jja_plan* p, jja_state* s, int nsteps, double* stage_ms, void*
     for (auto& e : ev) JJA_CUDA(cudaEventCreate(&e));
     JJA_CUDA(cudaEventRecord(ev[0], st));
     launch_scale_sources(p, s, st);
-    {
-      StepArgs a = make_args(p, s);
+    const std::vector<Group*> gs = step_groups(p);
+    for (Group* g : gs) {
+      StepArgs a = make_args(p, s, *g);
       launch_junction(p, a, st);
     }
+    // the groups one after another on the caller's stream, stage by stage, so the events time
+    // each stage of the whole step
     const int period = p->width - 1;
     for (int i = 0; i < nsteps; ++i) {
-      StepArgs a = make_args(p, s);
-      a.hout = s->hist[period - 1];
-      a.th_slot = a.I_slot = -1;
-      launch_step(p, a, st, i + 1 < nsteps, ev.data() + 1 + 5 * (size_t)i);
+      cudaEvent_t* e = ev.data() + 1 + 5 * (size_t)i;
+      std::vector<StepArgs> args;
+      for (Group* g : gs) {
+        args.push_back(make_args(p, s, *g));
+        args.back().hout = s->hist[period - 1];
+        args.back().th_slot = args.back().I_slot = -1;
+      }
+      JJA_CUDA(cudaEventRecord(e[0], st));
+      for (size_t k = 0; k < gs.size(); ++k)
+        launch(p->pdl, k_face_rhs, grid_for((int64_t)p->Nf * gs[k]->wn, 256), 256, st, args[k], p->t,
+               (const double*)p->xj, p->b);
+      JJA_CUDA(cudaEventRecord(e[1], st));
+      for (Group* g : gs) launch_levels(p, *g, st, true);
+      JJA_CUDA(cudaEventRecord(e[2], st));
+      for (Group* g : gs) launch_levels(p, *g, st, false);
+      JJA_CUDA(cudaEventRecord(e[3], st));
+      for (size_t k = 0; k < gs.size(); ++k) {
+        const int64_t nj = (int64_t)p->Nj * gs[k]->wn;
+        if (i + 1 < nsteps)
+          launch(p->pdl, k_update<true>, grid_for(nj, 256), 256, st, args[k], p->t, p->xj, (const double*)p->x);
+        else
+          launch(p->pdl, k_update<false>, grid_for(nj, 256), 256, st, args[k], p->t, p->xj, (const double*)p->x);
+      }
+      JJA_CUDA(cudaEventRecord(e[4], st));
       rotate(s, p->width);
     }
     JJA_CUDA(cudaEventSynchronize(ev.back()));

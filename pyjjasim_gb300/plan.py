@@ -26,7 +26,7 @@ MAX_PLANS = 4
 EXTRAP = {3: (2.0, -1.0), 4: (3.0, -3.0, 1.0), 5: (4.0, -6.0, 4.0, -1.0)}
 # launch-shape fields of the triangular solves (jja_solve_tuning)
 TUNING_FIELDS = ("rhs_block", "rows_per_lane", "target_warps", "min_piece", "schedule", "rows_per_lane_fwd",
-                 "pack_rows", "pack_min_warps", "pdl")
+                 "pack_rows", "pack_min_warps", "pdl", "groups")
 SCHEDULES = {"levels": 1, "dataflow": 2}
 
 

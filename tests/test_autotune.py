@@ -22,7 +22,7 @@ def test_coordinate_descent_finds_the_fastest_axis_values():
     best, t, log = AT.coordinate_descent(512, measure)
     assert best["rows_per_lane"] == 4 and best["target_warps"] == 152 * 8
     assert tuple(best["relax"]) == (-1, -1.0) and best["rhs_block"] == 0
-    assert best["schedule"] == 1 and best["ordering"] == "nd"
+    assert best["schedule"] == 1 and best["ordering"] == "auto" and best["groups"] == 0
     assert t == pytest.approx(0.72)
     cand = AT.candidates(512)
     n_tried = 1 + sum(int(np.prod([len(cand[n]) for n in (a if isinstance(a, tuple) else (a,))])) - 1
@@ -46,7 +46,7 @@ def test_cache_is_written_and_reused(tmp_path, monkeypatch):
         return 2.0 if cfg["rows_per_lane"] == 4 else 3.0
 
     opts = AT.autotune(c, 0.05, 4, measure=measure, device_name="fake-gpu")
-    assert opts["tuning"]["rows_per_lane"] == 4 and opts["relax"] == (-1, -1.0) and opts["ordering"] == "nd"
+    assert opts["tuning"]["rows_per_lane"] == 4 and opts["relax"] == (-1, -1.0) and opts["ordering"] == "auto"
     n = len(calls)
     again = AT.autotune(c, 0.05, 4, measure=measure, device_name="fake-gpu")
     assert again == opts and len(calls) == n             # served from the cache
@@ -68,6 +68,7 @@ def test_cache_is_written_and_reused(tmp_path, monkeypatch):
                                           ({"schedule": 2, "rows_per_lane": 2, "min_piece": 4,
                                             "target_warps": 152 * 200}, (64, 0.1)),
                                           ({"pdl": 1}, (-1, -1.0)),
+                                          ({"groups": 1}, (-1, -1.0)),
                                           ({"pdl": 1, "schedule": 2, "rows_per_lane": 4}, (0, 0.0))])
 def test_tuned_launch_shapes_agree_with_default(tuning, relax):
     from pyjjasim_gb300 import TimeEvolutionProblem, backend

@@ -154,17 +154,39 @@ def test_graph_and_eager_paths_agree():
     close(th_g, th_e, rtol=1e-11)
 
 
-def test_store_all_matches_per_step_slots():
+@pytest.mark.parametrize("groups", [2, 3])
+def test_problem_groups_match_one_chain(groups):
+    """The step run as independent groups of problems on their own streams (forked from and
+    joined back into the call's stream, inside and outside captured graphs) gives the one-chain
+    trajectory: thermal noise keyed by (junction-problem, step), time-dependent sources, stored
+    steps and the adjoint-style store_all path all see the same global problem index."""
+    c = SquareArray(21, 19)
+    c.set_inductance(0.1)
+    W, Nt = 96, 120
+    Is = lambda i: c.current_base(0.0)[:, None] * (np.linspace(0.2, 1.6, W)[None, :] + 0.1 * np.sin(0.05 * i))
+    prob = TimeEvolutionProblem(c, time_step=0.05, time_step_count=Nt, current_sources=Is, external_flux=0.2,
+                                temperature=0.01, store_time_steps=np.arange(0, Nt, 9))
+    th1, I1 = backend.time_evolution_core(prob, prob.store_time_steps, prob.store_time_steps, seed=5,
+                                          tuning={"groups": 1})
+    th2, I2 = backend.time_evolution_core(prob, prob.store_time_steps, prob.store_time_steps, seed=5,
+                                          tuning={"groups": groups})
+    close(th2, th1, rtol=1e-10)
+    close(I2, I1, rtol=1e-10)
+
+
+@pytest.mark.parametrize("W,groups", [(5, 0), (70, 3)])
+def test_store_all_matches_per_step_slots(W, groups):
     """Storing every step with slots derived on the device (graph replays) gives the same
-    phases and currents as per-step slots from the host (eager launches)."""
+    phases and currents as per-step slots from the host (eager launches), also with the step
+    split into groups of problems."""
     import torch
     c = SquareArray(17, 13)
-    W, L = 5, 150
+    L = 150
     Is = c.current_base(0.0)[:, None, None] * np.linspace(0.5, 1.5, W)[None, :, None]
     prob = TimeEvolutionProblem(c, time_step=0.05, time_step_count=L, current_sources=Is, external_flux=0.2)
     out = []
     for store_all in (False, True):
-        sim = backend.GpuSimulation(prob)
+        sim = backend.GpuSimulation(prob, tuning={"groups": groups})
         th = torch.empty((L, c.junction_count(), W), dtype=torch.float64, device=sim.dev)
         I = torch.empty_like(th)
         with torch.cuda.stream(sim.stream):
