@@ -194,8 +194,10 @@ int jja_run(jja_plan* p, jja_state* st, int nsteps, const int64_t* th_slot, cons
 
 /* Like jja_run (no stored outputs, no graph) but records CUDA events at the stage boundaries
  * of every step. stage_ms[6] receives the summed device time of: junction currents,
- * face right-hand side, forward solve, backward solve, update; and [5] the whole run.
- * Used by the benchmark to attribute step time to kernels; same results as jja_run. */
+ * face right-hand side, forward solve, backward solve, update; and [5] the whole run. With
+ * problem groups every stage runs the groups concurrently and joins them before its closing
+ * event (the stages do not overlap each other, as they do in jja_run). Used by the benchmark
+ * to attribute step time to kernels; same results as jja_run. */
 int jja_run_timed(jja_plan* p, jja_state* st, int nsteps, double* stage_ms, void* stream);
 
 /* ---------------------------------------------------------------------------- adjoint --- */

@@ -2236,12 +2236,14 @@ int jja_run_timed(jja_plan* p, jja_state* s, int nsteps, double* stage_ms, void*
     JJA_CUDA(cudaEventRecord(ev[0], st));
     launch_scale_sources(p, s, st);
     const std::vector<Group*> gs = step_groups(p);
+    fork_groups(p, st);
     for (Group* g : gs) {
       StepArgs a = make_args(p, s, *g);
-      launch_junction(p, a, st);
+      launch_junction(p, a, stream_of(*g, st));
     }
-    // the groups one after another on the caller's stream, stage by stage, so the events time
-    // each stage of the whole step
+    join_groups(p, st);
+    // stage by stage: the groups run each stage concurrently on their streams and join back
+    // into the caller's stream at every stage boundary, where the events are recorded
     const int period = p->width - 1;
     for (int i = 0; i < nsteps; ++i) {
       cudaEvent_t* e = ev.data() + 1 + 5 * (size_t)i;
@@ -2251,23 +2253,26 @@ int jja_run_timed(jja_plan* p, jja_state* s, int nsteps, double* stage_ms, void*
         args.back().hout = s->hist[period - 1];
         args.back().th_slot = args.back().I_slot = -1;
       }
+      auto stage = [&](int k, auto&& fn) {
+        fork_groups(p, st);
+        for (size_t q = 0; q < gs.size(); ++q) fn(q, stream_of(*gs[q], st));
+        join_groups(p, st);
+        JJA_CUDA(cudaEventRecord(e[k], st));
+      };
       JJA_CUDA(cudaEventRecord(e[0], st));
-      for (size_t k = 0; k < gs.size(); ++k)
-        launch(p->pdl, k_face_rhs, grid_for((int64_t)p->Nf * gs[k]->wn, 256), 256, st, args[k], p->t,
+      stage(1, [&](size_t q, cudaStream_t gst) {
+        launch(p->pdl, k_face_rhs, grid_for((int64_t)p->Nf * gs[q]->wn, 256), 256, gst, args[q], p->t,
                (const double*)p->xj, p->b);
-      JJA_CUDA(cudaEventRecord(e[1], st));
-      for (Group* g : gs) launch_levels(p, *g, st, true);
-      JJA_CUDA(cudaEventRecord(e[2], st));
-      for (Group* g : gs) launch_levels(p, *g, st, false);
-      JJA_CUDA(cudaEventRecord(e[3], st));
-      for (size_t k = 0; k < gs.size(); ++k) {
-        const int64_t nj = (int64_t)p->Nj * gs[k]->wn;
+      });
+      stage(2, [&](size_t q, cudaStream_t gst) { launch_levels(p, *gs[q], gst, true); });
+      stage(3, [&](size_t q, cudaStream_t gst) { launch_levels(p, *gs[q], gst, false); });
+      stage(4, [&](size_t q, cudaStream_t gst) {
+        const int64_t nj = (int64_t)p->Nj * gs[q]->wn;
         if (i + 1 < nsteps)
-          launch(p->pdl, k_update<true>, grid_for(nj, 256), 256, st, args[k], p->t, p->xj, (const double*)p->x);
+          launch(p->pdl, k_update<true>, grid_for(nj, 256), 256, gst, args[q], p->t, p->xj, (const double*)p->x);
         else
-          launch(p->pdl, k_update<false>, grid_for(nj, 256), 256, st, args[k], p->t, p->xj, (const double*)p->x);
-      }
-      JJA_CUDA(cudaEventRecord(e[4], st));
+          launch(p->pdl, k_update<false>, grid_for(nj, 256), 256, gst, args[q], p->t, p->xj, (const double*)p->x);
+      });
       rotate(s, p->width);
     }
     JJA_CUDA(cudaEventSynchronize(ev.back()));
