@@ -82,6 +82,7 @@ class Circuit:
         self.set_capacitance(capacitance)
         self.set_inductance(inductance)
         self._Msq_factorized = None
+        self._Asq_factorized = None
 
     # --- component setters (josephson_circuit.py:406-461, 595-604) -------------------------
     def set_critical_current(self, Ic):
@@ -195,6 +196,16 @@ class Circuit:
             self._Msq_factorized = scipy.sparse.linalg.factorized((Mr @ Mr.T).tocsc())
         b = np.asarray(b, dtype=np.float64)
         return np.append(self._Msq_factorized(b[:-1, ...]), np.zeros(b[-1:, ...].shape), axis=0)
+
+    def Asq_solve(self, b):
+        """Solves A A^T x = b (A the cycle matrix; josephson_circuit.py:111-128)."""
+        if self._Asq_factorized is None:
+            A = self.get_cycle_matrix()
+            self._Asq_factorized = scipy.sparse.linalg.factorized((A @ A.T).tocsc())
+        return self._Asq_factorized(np.asarray(b, dtype=np.float64))
+
+    def _has_capacitance(self):
+        return bool(np.any(self.capacitance > 0))
 
     def node_to_junction_current(self, node_current):
         return -(self.get_cut_matrix().T @ self.Msq_solve(node_current))

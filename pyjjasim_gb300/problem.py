@@ -196,6 +196,9 @@ class TimeEvolutionProblem:
     def _cp(self, theta):
         return self.current_phase_relation.eval(self.circuit._Ic()[:, None], theta)
 
+    def _icp(self, theta):
+        return self.current_phase_relation.i_eval(self.circuit._Ic()[:, None], theta)
+
     def _to_time_point_mask(self, time_points):
         if time_points is None:
             time_points = self.store_time_steps
@@ -337,9 +340,11 @@ class TimeEvolutionResult:
             raise CurrentNotStored("Cannot query current; quantity is not stored during time evolution simulation.")
         return self.current[:, :, self._time_point_index(tp)]
 
-    def _select(self, select_time_points, N, func):
+    def _select(self, select_time_points, N, func, is_zero=False):
         # filled time-major (contiguous copies) and returned as the (N, W, T) view
         sel = np.flatnonzero(self.problem._to_time_point_mask(select_time_points))
+        if is_zero:
+            return np.zeros((N, self.get_problem_count(), len(sel)), dtype=np.double)
         out = np.empty((len(sel), N, self.get_problem_count()), dtype=np.double)
         for k, tp in enumerate(sel):
             out[k] = func(tp)
@@ -353,6 +358,89 @@ class TimeEvolutionResult:
 
     def get_voltage(self, select_time_points=None):
         return self._select(select_time_points, self.get_circuit()._Nj(), self._V)
+
+    # observables derived from the stored quantities (time_evolution.py:692-985), same formulas
+    def get_phase(self, select_time_points=None):
+        """Node phases (Nn, W, T), last node grounded: solves M M^T phi = M theta (:692-714)."""
+        c = self.get_circuit()
+        M, Nj = c.get_cut_matrix(), c._Nj()
+        func = lambda tp: c.Msq_solve(M @ self._th(tp).reshape(Nj, -1))
+        try:
+            return self._select(select_time_points, c._Nn(), func)
+        except ThetaNotStored:
+            raise ThetaNotStored("Cannot compute phi; requires theta to be stored in TimeEvolutionConfig")
+
+    def get_josephson_energy(self, select_time_points=None):
+        """Ic (1 - cos theta) per junction (:757-777)."""
+        func = lambda tp: self.problem._icp(self._th(tp))
+        try:
+            return self._select(select_time_points, self.get_circuit()._Nj(), func)
+        except ThetaNotStored:
+            raise ThetaNotStored("Cannot compute Josephson energy EJ; requires theta to be stored in TimeEvolutionConfig")
+
+    def get_supercurrent(self, select_time_points=None):
+        """Ic sin theta per junction (:797-817)."""
+        func = lambda tp: self.problem._cp(self._th(tp))
+        try:
+            return self._select(select_time_points, self.get_circuit()._Nj(), func)
+        except ThetaNotStored:
+            raise ThetaNotStored("Cannot compute supercurrent Isup; requires theta to be stored in TimeEvolutionConfig")
+
+    def get_cycle_current(self, select_time_points=None):
+        """Cycle currents J with I = A^T J + Is: solves A A^T J = A (I - Is) (:819-841)."""
+        c = self.get_circuit()
+        A = c.get_cycle_matrix()
+        func = lambda tp: c.Asq_solve(A @ (self._I(tp) - self.problem._Is(tp)))
+        try:
+            return self._select(select_time_points, c._Nf(), func)
+        except CurrentNotStored:
+            raise CurrentNotStored("Cannot compute cycle-current J; requires current to be stored in TimeEvolutionConfig")
+
+    def get_flux(self, select_time_points=None):
+        """Flux through faces, f + A L I / (2 pi) (:843-866)."""
+        c = self.get_circuit()
+        A = c.get_cycle_matrix()
+        func = lambda tp: self.problem._f(tp) + A @ (c._L() @ self._I(tp)) / (2 * np.pi)
+        try:
+            return self._select(select_time_points, c._Nf(), func)
+        except CurrentNotStored:
+            raise CurrentNotStored("Cannot compute magnetic flux; requires current to be stored in TimeEvolutionConfig")
+
+    def get_magnetic_energy(self, select_time_points=None):
+        """L I^2 / 2 per junction (:868-890)."""
+        c = self.get_circuit()
+        func = lambda tp: 0.5 * c._L() @ (self._I(tp) ** 2)
+        try:
+            return self._select(select_time_points, c._Nj(), func, is_zero=not c._has_inductance())
+        except CurrentNotStored:
+            raise CurrentNotStored("Cannot compute magnetic energy EM; requires current to be stored in TimeEvolutionConfig")
+
+    def get_potential(self, select_time_points=None):
+        """Node potentials (Nn, W, T), last node grounded: solves M M^T U = M V (:910-937)."""
+        c = self.get_circuit()
+        M, Nj = c.get_cut_matrix(), c._Nj()
+        func = lambda tp: c.Msq_solve(M @ self._V(tp).reshape(Nj, -1))
+        try:
+            return self._select(select_time_points, c._Nn(), func)
+        except VoltageNotStored:
+            raise VoltageNotStored("Cannot compute electric potential U; requires voltage to be stored in "
+                                   "TimeEvolutionConfig")
+
+    def get_capacitive_energy(self, select_time_points=None):
+        """C V^2 / 2 per junction (:939-963)."""
+        c = self.get_circuit()
+        C = c._C()
+        func = lambda tp: 0.5 * C[:, None] * self._V(tp) ** 2
+        try:
+            return self._select(select_time_points, c._Nj(), func, is_zero=not c._has_capacitance())
+        except VoltageNotStored:
+            raise VoltageNotStored("Cannot compute capacitive energy EC; requires voltage to be stored in "
+                                   "TimeEvolutionConfig")
+
+    def get_energy(self, select_time_points=None):
+        """Josephson + magnetic + capacitive energy per junction (:965-985)."""
+        return self.get_josephson_energy(select_time_points) + self.get_magnetic_energy(select_time_points) + \
+            self.get_capacitive_energy(select_time_points)
 
     def get_vortex_configuration(self, select_time_points=None):
         A = self.get_circuit().get_cycle_matrix()

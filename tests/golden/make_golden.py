@@ -13,8 +13,9 @@ modified; bytecode writing is disabled so its read-only tree is never touched.
 
 Each fixture holds the exact inputs (cycle matrix A, component vectors, source arrays or
 the parameters of a source callable, seeds, store masks) and the reference outputs
-(theta, current, voltage at the stored steps, and the vortex configuration), so a test
-can rebuild the same problem with no reference present.
+(theta, current, voltage at the stored steps, the vortex configuration, and the result's
+derived observables: node phases and potentials, cycle currents, flux, supercurrent and the
+energies), so a test can rebuild the same problem with no reference present.
 
 Usage:  python tests/golden/make_golden.py [--ref /root/reference]
 """
@@ -88,6 +89,10 @@ def run_case(pj, name, circuit, dt, Nt, *, f=0.0, Is=0.0, Vs=0.0, T=0.0, seed=No
              seed=np.int64(-1 if seed is None else seed), store_mask=prob.get_store_time_steps().copy(),
              theta=res.get_theta(), current=res.current.copy(), voltage=res.get_voltage(),
              vortex=res.get_vortex_configuration())
+    # the result's derived observables (time_evolution.py:692-985) at every stored step
+    for obs in ("phase", "josephson_energy", "supercurrent", "cycle_current", "flux", "magnetic_energy", "potential",
+                "capacitive_energy", "energy"):
+        d["obs_" + obs] = np.asarray(getattr(res, "get_" + obs)(), dtype=np.float64)
     # inputs: arrays stored compact (before broadcasting); callables by their parameters
     for key, val in (("f", f), ("Is", Is), ("Vs", Vs), ("T", T)):
         if callable(val):
