@@ -12,7 +12,10 @@ unchanged here, with the per-step core executed on the GPU:
   voltage stencil has its previous steps, calls the core, derives V, strips helper
   steps. The core is the GPU backend (``pyjjasim_gb300.backend.time_evolution_core``).
 * ``TimeEvolutionResult`` (time_evolution.py:597-1067): theta / current / voltage /
-  vortex configuration accessors with the same shapes and errors.
+  vortex configuration accessors and the derived observables (node phases and potentials,
+  cycle currents, flux, supercurrent, energies; :692-985) with the same shapes and errors.
+  For results of the GPU core the node-space solves of the phases and potentials run on the
+  GPU (``pyjjasim_gb300.observables``).
 """
 import numpy as np
 
@@ -243,6 +246,7 @@ def time_evolution(problem, core=None, **options):
 
     ``core`` replaces the GPU core with another function of the same signature (tests use
     this to check the masks and post-processing on a machine without a GPU)."""
+    on_device = core is None
     if core is None:
         from .backend import time_evolution_core as core
     Nt = problem._Nt()
@@ -277,7 +281,9 @@ def time_evolution(problem, core=None, **options):
     I_keep = offset + np.flatnonzero(I_mask[VI_mask])
     th_out = _select_slots(th_out, th_keep) if problem.store_theta else None
     I_out = _select_slots(I_out, I_keep) if problem.store_current else None
-    return TimeEvolutionResult(problem, th_out, I_out, V)
+    res = TimeEvolutionResult(problem, th_out, I_out, V)
+    res.node_solves_on_device = on_device
+    return res
 
 
 class ThetaNotStored(Exception):
@@ -311,6 +317,16 @@ class TimeEvolutionResult:
         self.voltage = voltage if problem.store_voltage else None
         s = problem.store_time_steps.astype(int)
         self.time_point_indices = np.cumsum(s) - s
+        # node phases / potentials solve M_r M_r^T x = b: with the GPU core's results on the GPU
+        # (pyjjasim_gb300.observables), else with SuperLU on the host as the reference does
+        self.node_solves_on_device = False
+
+    def _msq_solve(self, b):
+        c = self.get_circuit()
+        if self.node_solves_on_device:
+            from .observables import msq_solve
+            return msq_solve(c, b)
+        return c.Msq_solve(b)
 
     def get_problem_count(self):
         return self.problem.get_problem_count()
@@ -364,7 +380,7 @@ class TimeEvolutionResult:
         """Node phases (Nn, W, T), last node grounded: solves M M^T phi = M theta (:692-714)."""
         c = self.get_circuit()
         M, Nj = c.get_cut_matrix(), c._Nj()
-        func = lambda tp: c.Msq_solve(M @ self._th(tp).reshape(Nj, -1))
+        func = lambda tp: self._msq_solve(M @ self._th(tp).reshape(Nj, -1))
         try:
             return self._select(select_time_points, c._Nn(), func)
         except ThetaNotStored:
@@ -419,7 +435,7 @@ class TimeEvolutionResult:
         """Node potentials (Nn, W, T), last node grounded: solves M M^T U = M V (:910-937)."""
         c = self.get_circuit()
         M, Nj = c.get_cut_matrix(), c._Nj()
-        func = lambda tp: c.Msq_solve(M @ self._V(tp).reshape(Nj, -1))
+        func = lambda tp: self._msq_solve(M @ self._V(tp).reshape(Nj, -1))
         try:
             return self._select(select_time_points, c._Nn(), func)
         except VoltageNotStored:

@@ -76,6 +76,19 @@ def test_face_solve_w1_packs(make, ordering, pack_rows):
     close(x, x0, rtol=1e-12)
 
 
+@pytest.mark.parametrize("make", [lambda: SquareArray(40, 33), lambda: HoneycombArray(12, 9),
+                                  lambda: TriangularArray(15, 14)])
+def test_node_space_solve_on_device(make):
+    """Node phases of a GPU result: the node-space solve M_r M_r^T x = M_r y on the GPU against
+    SuperLU on the host (the reference's Circuit.Msq_solve), last node grounded."""
+    from pyjjasim_gb300 import observables
+    c = make()
+    y = np.random.default_rng(4).standard_normal((c.junction_count(), 7))
+    b = c.get_cut_matrix() @ y
+    close(observables.msq_solve(c, b), c.Msq_solve(b), rtol=1e-11)
+    close(observables.msq_solve(c, b[:, 0]), c.Msq_solve(b[:, 0]), rtol=1e-11)
+
+
 def _mixed_problem(c, W, Nt, seed):
     rng = np.random.default_rng(seed)
     Nj, Nf = c.junction_count(), c.face_count()
