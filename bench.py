@@ -280,7 +280,6 @@ def ragged_leg(G, torch, n_problems, steps):
     honeycomb / triangular and side n ~ U{32..256}, bias linspace(0, 2, 256)[k] on
     current_base(0) of problem k, f = 0.25, T = 0, dt = 0.05; the first `n_problems` of the 256
     draws run as one block-diagonal system. `steps` graph-replayed steps timed with CUDA events."""
-    from pyjjasim_gb300.backend import GpuSimulation
     from pyjjasim_gb300.ragged import RaggedBatch
     rng = np.random.default_rng(7)
     kinds, sizes = rng.integers(0, 3, 256), rng.integers(32, 257, 256)
@@ -294,15 +293,35 @@ def ragged_leg(G, torch, n_problems, steps):
                                             current_sources=c.current_base(0.0)[:, None, None] * b,
                                             external_flux=0.25, store_time_steps=[steps + 63]))
     rb = RaggedBatch(probs)
-    sim = GpuSimulation(rb.union_problem())
-    sim.synchronize()
+    sims = rb.simulations()
+    for sim in sims:
+        sim.synchronize()
     t_setup = time.perf_counter() - t0
-    el = _timed_steps(torch, sim, steps)
+    # the parts step concurrently on their own streams (one host thread each): fork from and
+    # join into one timing stream
+    main = torch.cuda.current_stream()
+    RaggedBatch.run_simulations(sims, 16 * (sims[0].width - 1) + 1)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(main)
+    for sim in sims:
+        sim.stream.wait_event(e0)
+    RaggedBatch.run_simulations(sims, steps)
+    for sim in sims:
+        done = torch.cuda.Event()
+        done.record(sim.stream)
+        main.wait_event(done)
+    e1.record(main)
+    e1.synchronize()
+    for sim in sims:
+        sim.synchronize()
+    el = e0.elapsed_time(e1) / 1e3
     return {"workload": f"ragged: first {n_problems} of 256 seeded problems (square/honeycomb/triangular, side "
-                        f"32-256), f=0.25, bias linspace(0,2,256), T=0, dt=0.05, one block-diagonal system",
-            "problems": n_problems, "Nj_total": rb.Nj, "Nf_total": rb.Nf, "steps": steps,
+                        f"32-256), f=0.25, bias linspace(0,2,256), T=0, dt=0.05, block-diagonal systems "
+                        f"({len(sims)} parts stepped concurrently)",
+            "problems": n_problems, "parts": len(sims), "Nj_total": rb.Nj, "Nf_total": rb.Nf, "steps": steps,
             "ms_per_step": el / steps * 1e3, "value": rb.Nj * steps / el, "unit": "junction-steps/s",
-            "setup_seconds": t_setup, "finite": bool(torch.isfinite(sim.theta()).all()),
+            "setup_seconds": t_setup, "finite": all(bool(torch.isfinite(s.theta()).all()) for s in sims),
             "lattices": [[["square", "honeycomb", "triangular"][int(k)], int(nn)]
                          for k, nn in list(zip(kinds, sizes))[:n_problems]]}
 

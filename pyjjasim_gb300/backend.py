@@ -363,15 +363,19 @@ class GpuSimulation:
 
 def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", seed=None, device=None,
                         use_graph=True, nd_leaf=8, stream=None, ordering="auto", relax=(-1, -1.0), Ic=None,
-                        tuning=None, tune=False):
+                        tuning=None, tune=False, sim=None):
     """GPU time-stepping core; see the module docstring for the contract.
 
     ``ordering`` ("nd", "mmd" or "auto": minimum degree when W x Nf >= 2^22 on up to 2^18 faces,
     nested dissection otherwise) and ``relax`` ((max zeros, max fraction) of supernode
     amalgamation; negative = library defaults) select how the face-space matrix is factorised;
-    ``tuning`` the solve's launch shape; ``tune=True`` lets the autotuner pick both."""
-    sim = GpuSimulation(problem, noise=noise, seed=seed, device=device, nd_leaf=nd_leaf, stream=stream,
-                        ordering=ordering, relax=relax, Ic=Ic, tuning=tuning, tune=tune)
+    ``tuning`` the solve's launch shape; ``tune=True`` lets the autotuner pick both. ``sim``: a
+    GpuSimulation of this problem, already built (its own options apply)."""
+    if sim is None:
+        sim = GpuSimulation(problem, noise=noise, seed=seed, device=device, nd_leaf=nd_leaf, stream=stream,
+                            ordering=ordering, relax=relax, Ic=Ic, tuning=tuning, tune=tune)
+    elif sim.problem is not problem:
+        raise ValueError("time_evolution_core: the simulation belongs to another problem")
     torch = sim.torch
     Nj, W, Nt, width = sim.Nj, sim.W, problem._Nt(), sim.width
     th_store_mask = np.asarray(th_store_mask, bool)

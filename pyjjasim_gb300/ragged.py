@@ -9,9 +9,17 @@ face-space matrix are block diagonal, so one nested-dissection factorisation yie
 whose trees' levels are merged, and every time step is one sequence of level launches over all
 problems at once, with the per-problem state laid out back to back (W = 1 in the union).
 
+Large batches are split into a few parts of about equal size, each its own union, factor and
+simulation, stepped concurrently on their own streams: each part's launch chain fills the SMs
+the other leaves idle at its latency-bound levels (measured on GB300, 32 problems with 4.5M
+junctions: one union 1.81 ms per step, two concurrent parts 1.20 ms).
+
 Restrictions: all problems share the time step, step count, stencil width and store mask
 (``RaggedBatch`` raises otherwise), and use the default current-phase relation.
 """
+import functools
+import threading
+
 import numpy as np
 import scipy.sparse
 
@@ -19,6 +27,28 @@ from .circuit import Circuit
 from .problem import TimeEvolutionProblem, TimeEvolutionResult, time_evolution
 
 __all__ = ["RaggedBatch"]
+
+PART_FROM_JUNCTIONS = 1 << 20    # batches of at least this many junctions (all copies) split in two
+_SEED_STRIDE = 0x632BE59BD9B4E019   # parts draw thermal noise from distinct Philox streams
+
+
+def _in_threads(fns):
+    """Call every function in its own thread; re-raise the first exception in the caller."""
+    errors = []
+
+    def guard(fn):
+        try:
+            fn()
+        except BaseException as e:
+            errors.append(e)
+
+    threads = [threading.Thread(target=guard, args=(fn,)) for fn in fns]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errors:
+        raise errors[0]
 
 
 def _geometry(c):
@@ -30,9 +60,12 @@ def _geometry(c):
 
 
 class RaggedBatch:
-    """A list of TimeEvolutionProblems (any circuits) computed together on the GPU."""
+    """A list of TimeEvolutionProblems (any circuits) computed together on the GPU.
 
-    def __init__(self, problems):
+    ``parts``: the number of concurrent unions (default: 2 from 2^20 junctions on, else 1);
+    problems are assigned whole, largest first, to the part with the fewest junctions."""
+
+    def __init__(self, problems, parts=None):
         if not problems:
             raise ValueError("empty batch")
         p0 = problems[0]
@@ -45,7 +78,24 @@ class RaggedBatch:
                                                                      p0.store_voltage):
                 raise ValueError("all problems of a ragged batch need the same store flags")
         self.problems = list(problems)
-        self._build_union()
+        size = [p.get_circuit()._Nj() * p.get_problem_count() for p in self.problems]
+        if parts is None:
+            parts = 2 if sum(size) >= PART_FROM_JUNCTIONS and len(self.problems) > 1 else 1
+        parts = max(1, min(int(parts), len(self.problems)))
+        if parts == 1:
+            self._build_union()
+            self.parts = [self]
+            return
+        load = [0] * parts
+        members = [[] for _ in range(parts)]
+        for i in sorted(range(len(self.problems)), key=lambda i: -size[i]):
+            k = int(np.argmin(load))
+            members[k].append(i)
+            load[k] += size[i]
+        self.part_members = [sorted(m) for m in members]
+        self.parts = [RaggedBatch([self.problems[i] for i in m], parts=1) for m in self.part_members]
+        self.Nj = sum(q.Nj for q in self.parts)
+        self.Nf = sum(q.Nf for q in self.parts)
 
     # the union of all (problem, w) copies -------------------------------------------------
     def _build_union(self):
@@ -102,6 +152,9 @@ class RaggedBatch:
         return at(0)[:, None, None]
 
     def union_problem(self):
+        """The union of all problems as one TimeEvolutionProblem (W = 1): a batch of one part."""
+        if len(self.parts) > 1:
+            raise ValueError("this batch runs as several parts: use parts[k].union_problem() or simulations()")
         p0 = self.problems[0]
         nj = lambda p: p.get_circuit()._Nj()
         nf = lambda p: p.get_circuit()._Nf()
@@ -121,14 +174,60 @@ class RaggedBatch:
             store_time_steps=p0.store_time_steps, store_theta=p0.store_theta, store_voltage=p0.store_voltage,
             store_current=p0.store_current, stencil_width=p0.stencil_width, **hist)
 
-    def compute(self, **options):
-        """Step all problems together; returns one TimeEvolutionResult per input problem."""
-        res = time_evolution(self.union_problem(), **options)
+    def _split(self, res):
+        """Per-problem results of this union's result."""
         out = []
         for p, per_w in zip(self.problems, self.slices):
             def gather(arr):
                 if arr is None:
                     return None
                 return np.stack([arr[js, 0, :] for js, _ in per_w], axis=1)
-            out.append(TimeEvolutionResult(p, gather(res.theta), gather(res.current), gather(res.voltage)))
+            r = TimeEvolutionResult(p, gather(res.theta), gather(res.current), gather(res.voltage))
+            r.node_solves_on_device = getattr(res, "node_solves_on_device", False)
+            out.append(r)
+        return out
+
+    def simulations(self, seed=None, **options):
+        """One GpuSimulation per part (each on its own stream), over the parts' union problems;
+        ``options`` as for GpuSimulation. The parts draw noise from distinct Philox streams."""
+        from .backend import GpuSimulation
+        sims = []
+        for k, part in enumerate(self.parts):
+            s = None if seed is None else (int(seed) + _SEED_STRIDE * k) % (1 << 63)
+            sims.append(GpuSimulation(part.union_problem(), seed=s, **options))
+        return sims
+
+    @staticmethod
+    def run_simulations(sims, nsteps, use_graph=True):
+        """Advance every part's simulation by nsteps steps, each from its own host thread: a long
+        run blocks its caller while the GPU drains the queued graph launches, so one thread per
+        part keeps all parts' launch chains queued together."""
+        _in_threads([lambda s=s: s.run(nsteps, use_graph=use_graph) for s in sims])
+
+    def compute(self, **options):
+        """Step all problems; returns one TimeEvolutionResult per input problem. With several
+        parts, each part's core runs in its own host thread, so their launch chains overlap."""
+        if len(self.parts) == 1:
+            return self._split(time_evolution(self.union_problem(), **options))
+        if "core" in options:            # a replacement core (tests): the parts one after another
+            results = [part._split(time_evolution(part.union_problem(), **options)) for part in self.parts]
+        else:
+            from .backend import time_evolution_core
+            opts = dict(options)
+            use_graph = opts.pop("use_graph", True)
+            sims = self.simulations(**opts)
+            results = [None] * len(sims)
+
+            def work(k):
+                core = functools.partial(time_evolution_core, sim=sims[k], use_graph=use_graph)
+                results[k] = self.parts[k]._split(time_evolution(sims[k].problem, core=core))
+
+            _in_threads([functools.partial(work, k) for k in range(len(sims))])
+            for r in results:
+                for x in r:
+                    x.node_solves_on_device = True
+        out = [None] * len(self.problems)
+        for members, res in zip(self.part_members, results):
+            for i, r in zip(members, res):
+                out[i] = r
         return out

@@ -40,12 +40,22 @@ def _check(results, problems, rtol):
                               rcsj_oracle.vortex_configuration(p.get_circuit().get_cycle_matrix(), th))
 
 
-def test_union_layout_with_oracle_core():
+@pytest.mark.parametrize("parts", [1, 2, 3])
+def test_union_layout_with_oracle_core(parts):
     problems = _problems()
-    batch = RaggedBatch(problems)
+    batch = RaggedBatch(problems, parts=parts)
+    assert len(batch.parts) == parts
     assert batch.Nj == sum(p.get_circuit()._Nj() * p.get_problem_count() for p in problems)
     assert batch.Nf == sum(p.get_circuit()._Nf() * p.get_problem_count() for p in problems)
+    if parts > 1:   # every problem in exactly one part, the parts balanced by junction count
+        assert sorted(i for m in batch.part_members for i in m) == list(range(len(problems)))
+        with pytest.raises(ValueError):
+            batch.union_problem()
     _check(batch.compute(core=rcsj_oracle.evolve), problems, rtol=1e-11)
+
+
+def test_default_parts():
+    assert len(RaggedBatch(_problems()).parts) == 1       # small batches stay one union
 
 
 def test_mismatched_problems_rejected():
@@ -55,6 +65,7 @@ def test_mismatched_problems_rejected():
 
 
 @pytest.mark.gpu
-def test_ragged_batch_on_gpu():
+@pytest.mark.parametrize("parts", [1, 2])
+def test_ragged_batch_on_gpu(parts):
     problems = _problems()
-    _check(RaggedBatch(problems).compute(), problems, rtol=1e-9)
+    _check(RaggedBatch(problems, parts=parts).compute(), problems, rtol=1e-9)
