@@ -231,6 +231,19 @@ def ac_driven_leg(G, torch, Nt, parity_steps=200):
            "Nj": Nj, "steps": Nt, "seconds": t, "value": Nj * Nt / t, "unit": "junction-steps/s",
            "timing": "end to end through compute(), host callable evaluated per step inside the timed region",
            "finite": bool(np.isfinite(V).all())}
+    # device time of the same steps (CUDA events on the simulation's stream, graph replays; the
+    # host fills the next window of the callable's values while the GPU runs the current one)
+    from pyjjasim_gb300.backend import GpuSimulation
+    dev = {}
+    for mode, tuning in (("levels", None), ("levels_pdl", {"pdl": 1}), ("dataflow", {"schedule": 2}),
+                         ("dataflow_pdl", {"schedule": 2, "pdl": 1})):
+        sim = GpuSimulation(problem(4096, [4095]), seed=2, tuning=tuning)
+        dev[mode] = _timed_steps(torch, sim, 2048) / 2048 * 1e3
+        del sim
+    best = min(dev, key=dev.get)
+    out["device"] = {"ms_per_step_by_schedule": dev, "best": best, "ms_per_step": dev[best],
+                     "value": Nj / (dev[best] / 1e3), "unit": "junction-steps/s",
+                     "timing": "CUDA events around 2048 graph-replayed steps"}
     if parity_steps:
         po = problem(parity_steps, [parity_steps - 2, parity_steps - 1])
         np.random.seed(11)
@@ -243,56 +256,82 @@ def ac_driven_leg(G, torch, Nt, parity_steps=200):
     return out
 
 
-def large_array_leg(G, torch, steps):
+def _lattice_base(kind, n):
+    """current_base(0) of a square (0), honeycomb (1) or triangular (2) array of side n: the
+    reference's uniform-bias pattern (one node-space solve; run in a worker process)."""
+    import pyjjasim_gb300 as G
+    return [G.SquareArray, G.HoneycombArray, G.TriangularArray][kind](int(n), int(n)).current_base(0.0)
+
+
+LARGE_BIAS = np.linspace(0.5, 1.2, 8)
+LARGE_PARITY_STEPS = 24
+
+
+def large_array_leg(G, torch, steps, base, oracle_job=None):
     """The large single array: SquareArray(1024,1024) (2.1M junctions), beta_C = 0.5, L = 0.05,
-    f = 0.1, 8 DC bias values 0.5-1.2 in one batch, T = 0.005 with on-device Philox noise,
-    dt = 0.05. The bias pattern is unit current on the horizontal junctions, which is what
-    current_base(0) gives for a square array up to ~1e-14 (its node-space solve alone takes
-    ~17 s at this size). `steps` graph-replayed steps are timed with CUDA events."""
+    f = 0.1, 8 DC bias values 0.5-1.2 on current_base(0) (the reference's pattern, computed by
+    its node-space solve in a worker), one batch, T = 0.005 with on-device Philox noise,
+    dt = 0.05. `steps` graph-replayed steps are timed with CUDA events. Parity: the same batch
+    at T = 0 for LARGE_PARITY_STEPS steps against the oracle (run in a worker process)."""
+    from oracle import parity_jobs as PJ
     from pyjjasim_gb300.backend import GpuSimulation
-    n = 1024
     t0 = time.perf_counter()
-    a = G.SquareArray(n, n)
-    a.set_capacitance(0.5)
-    a.set_inductance(0.05)
-    base = np.concatenate([np.ones(n * (n - 1)), np.zeros(n * (n - 1))])
-    bias = np.linspace(0.5, 1.2, 8)
-    p = G.TimeEvolutionProblem(a, time_step=0.05, time_step_count=10000,
-                               current_sources=base[:, None, None] * bias[None, :, None], external_flux=0.1,
-                               temperature=0.005, store_time_steps=[9999])
+    p = PJ.large_array_problem(G, LARGE_BIAS, 10000, base=base, temperature=0.005)
     sim = GpuSimulation(p, seed=3)
     sim.synchronize()
     t_plan = time.perf_counter() - t0
     el = _timed_steps(torch, sim, steps)
-    Nj, W = a._Nj(), 8
+    a = p.get_circuit()
+    Nj, W = a._Nj(), len(LARGE_BIAS)
     from pyjjasim_gb300 import plan as P
     fstats = list(P._FACTORS.values())[-1][0].stats if P._FACTORS else None   # the most recent factor
-    return {"workload": "SquareArray(1024,1024), C=0.5, L=0.05, f=0.1, bias linspace(0.5,1.2,8) on the horizontal "
-                        "junctions, T=0.005 (Philox), dt=0.05, W=8",
-            "Nj": Nj, "W": W, "steps": steps, "ms_per_step": el / steps * 1e3, "value": Nj * W * steps / el,
-            "unit": "junction-steps/s", "setup_seconds": t_plan, "device_bytes": int(sim.plan.device_bytes),
-            "factor": {k: fstats[k] for k in ("nnz_L", "n_levels", "max_k")} if fstats else None,
-            "finite": bool(torch.isfinite(sim.theta()).all())}
+    out = {"workload": "SquareArray(1024,1024), C=0.5, L=0.05, f=0.1, bias linspace(0.5,1.2,8) x current_base(0), "
+                       "T=0.005 (Philox), dt=0.05, W=8",
+           "Nj": Nj, "W": W, "steps": steps, "ms_per_step": el / steps * 1e3, "value": Nj * W * steps / el,
+           "unit": "junction-steps/s", "setup_seconds": t_plan, "device_bytes": int(sim.plan.device_bytes),
+           "factor": {k: fstats[k] for k in ("nnz_L", "n_levels", "max_k")} if fstats else None,
+           "finite": bool(torch.isfinite(sim.theta()).all())}
+    del sim
+    if oracle_job is not None:
+        S = LARGE_PARITY_STEPS
+        res = PJ.large_array_problem(G, LARGE_BIAS, S, base=base).compute()
+        th_g = res.get_theta()
+        th_o, _ = oracle_job.get()
+        err = float(np.abs(th_g - th_o).max())
+        scale = max(1.0, float(np.abs(th_o).max()))
+        out["parity"] = {"steps": S, "temperature": 0.0, "W": W, "max_abs_theta_error": err,
+                         "rel_theta": err / scale, "tolerance": 1e-9, "within_tolerance": bool(err <= 1e-9 * scale),
+                         "oracle": "numpy/scipy restatement of the reference loop on the same problem (SuperLU)"}
+    return out
 
 
-def ragged_leg(G, torch, n_problems, steps):
+def ragged_draws():
+    """The ragged batch's seeded draws: lattice kind (square / honeycomb / triangular) and side."""
+    rng = np.random.default_rng(7)
+    return rng.integers(0, 3, 256), rng.integers(32, 257, 256)
+
+
+def ragged_leg(G, torch, n_problems, steps, bases):
     """The ragged batch: problems drawn (seeded) with lattice type uniform over square /
     honeycomb / triangular and side n ~ U{32..256}, bias linspace(0, 2, 256)[k] on
-    current_base(0) of problem k, f = 0.25, T = 0, dt = 0.05; the first `n_problems` of the 256
-    draws run as one block-diagonal system. `steps` graph-replayed steps timed with CUDA events."""
+    current_base(0) of problem k (`bases`, computed in worker processes), f = 0.25, T = 0,
+    dt = 0.05; the first `n_problems` of the 256 draws run as block-diagonal systems in
+    concurrent parts. `steps` graph-replayed steps timed with CUDA events."""
     from pyjjasim_gb300.ragged import RaggedBatch
-    rng = np.random.default_rng(7)
-    kinds, sizes = rng.integers(0, 3, 256), rng.integers(32, 257, 256)
+    kinds, sizes = ragged_draws()
     bias = np.linspace(0.0, 2.0, 256)
     lattices = (G.SquareArray, G.HoneycombArray, G.TriangularArray)
     t0 = time.perf_counter()
     probs = []
     for k, nn, b in list(zip(kinds, sizes, bias))[:n_problems]:
         c = lattices[k](int(nn), int(nn))
+        base = bases[(int(k), int(nn))]
         probs.append(G.TimeEvolutionProblem(c, time_step=0.05, time_step_count=steps + 64,
-                                            current_sources=c.current_base(0.0)[:, None, None] * b,
+                                            current_sources=base[:, None, None] * b,
                                             external_flux=0.25, store_time_steps=[steps + 63]))
+    t_problems = time.perf_counter() - t0
     rb = RaggedBatch(probs)
+    t_union = time.perf_counter() - t0 - t_problems
     sims = rb.simulations()
     for sim in sims:
         sim.synchronize()
@@ -316,53 +355,116 @@ def ragged_leg(G, torch, n_problems, steps):
     for sim in sims:
         sim.synchronize()
     el = e0.elapsed_time(e1) / 1e3
-    return {"workload": f"ragged: first {n_problems} of 256 seeded problems (square/honeycomb/triangular, side "
-                        f"32-256), f=0.25, bias linspace(0,2,256), T=0, dt=0.05, block-diagonal systems "
-                        f"({len(sims)} parts stepped concurrently)",
+    from collections import Counter
+    kinds_used = Counter(["square", "honeycomb", "triangular"][int(k)] for k in kinds[:n_problems])
+    return {"workload": f"ragged: {n_problems} of 256 seeded problems (square/honeycomb/triangular, side "
+                        f"32-256), f=0.25, bias linspace(0,2,256) x current_base(0), T=0, dt=0.05, block-diagonal "
+                        f"systems ({len(sims)} parts stepped concurrently)",
             "problems": n_problems, "parts": len(sims), "Nj_total": rb.Nj, "Nf_total": rb.Nf, "steps": steps,
             "ms_per_step": el / steps * 1e3, "value": rb.Nj * steps / el, "unit": "junction-steps/s",
-            "setup_seconds": t_setup, "finite": all(bool(torch.isfinite(s.theta()).all()) for s in sims),
-            "lattices": [[["square", "honeycomb", "triangular"][int(k)], int(nn)]
-                         for k, nn in list(zip(kinds, sizes))[:n_problems]]}
+            "setup_seconds": t_setup,
+            "setup_breakdown_seconds": {"problems": t_problems, "unions": t_union,
+                                        "factor_and_plans": t_setup - t_problems - t_union},
+            "device_bytes": int(sum(s.plan.device_bytes for s in sims)),
+            "finite": all(bool(torch.isfinite(s.theta()).all()) for s in sims),
+            "lattice_kinds": dict(kinds_used)}
 
 
-PARITY_PROBLEMS = (150, 250, 350, 450)   # bias 0.59, 0.98, 1.37, 1.76: across the IV curve
+PARITY_PROBLEMS = (100, 150, 250, 350, 450, 511)   # bias 0.39 ... 2.0: across the IV curve
+THETA_STEPS = 2000          # trajectories are compared after this many steps (1e-9 relative bar)
 
 
-def parity_leg(G, Nt):
-    """Error of the batched GPU run against the FP64 CPU oracle on the headline workload:
-    all 512 problems on the GPU for Nt steps, four of them (PARITY_PROBLEMS) in the oracle;
-    time-averaged voltage of the horizontal junctions over the second half (the IV-curve
-    point), trajectories, and vortex configurations at the last step."""
+def start_oracle_jobs(args, pool):
+    """Oracle runs of the parity legs, submitted to a pool of spawned worker processes so they
+    overlap the GPU legs. Returns the pending results."""
+    from oracle import parity_jobs as PJ
+    jobs = {}
+    if args.parity_steps > 0:
+        bias = bias_slice(0, 1)
+        Np = args.parity_steps
+        t_th = min(THETA_STEPS, Np)
+        store = sorted({t_th - 1, Np // 2 - 1, Np - 1})
+        jobs["iv"] = {p: pool.apply_async(PJ.iv_sweep_theta, (float(bias[p]), Np, store)) for p in PARITY_PROBLEMS}
+        jobs["iv_alt"] = {p: pool.apply_async(PJ.iv_sweep_theta, (float(bias[p]), t_th, [t_th - 1], True))
+                          for p in PARITY_PROBLEMS}
+        jobs["iv_store"] = store
+    if args.large_steps > 0:
+        jobs["large_base"] = pool.apply_async(_lattice_base, (0, 1024))
+        if args.parity_steps > 0:
+            jobs["large"] = pool.apply_async(PJ.large_array_theta, (LARGE_BIAS, LARGE_PARITY_STEPS,
+                                                                    [LARGE_PARITY_STEPS - 1]))
+    if args.ragged_problems > 0:
+        kinds, sizes = ragged_draws()
+        keys = sorted({(int(k), int(n)) for k, n in list(zip(kinds, sizes))[:args.ragged_problems]})
+        jobs["ragged_bases"] = {key: pool.apply_async(_lattice_base, key) for key in keys}
+    return jobs
+
+
+def parity_leg(G, args, jobs, th_e2e=None):
+    """Error of the batched GPU run against the FP64 CPU oracle on the headline workload
+    (W = 512 x SquareArray(128,128), f = 0.25, bias linspace(0,2,512)), at its real length:
+    * trajectories after THETA_STEPS steps, relative max |dtheta| / max(1, |theta|) per problem
+      against the 1e-9 bar, beside the oracle's own spread: the same oracle with SuperLU's MMD
+      column order instead of COLAMD (same algorithm, another rounding) after as many steps;
+    * the IV-curve point of the e2e workload: V-bar = mean over horizontal junctions of
+      (theta_9999 - theta_4999) / (dt 5000), per problem, against the 1e-6 tolerance;
+    * vortex configurations at the last step.
+    All 512 problems run on the GPU; PARITY_PROBLEMS run in the oracle (worker processes).
+    ``th_e2e``: the e2e call's phases at steps Np/2 - 1 and Np - 1 (Nj, 512, 2), when it ran
+    the same workload; otherwise the GPU run is made here."""
     from oracle import rcsj_oracle
-    t1, t2 = Nt // 2 - 1, Nt - 1
+    Np = args.parity_steps
+    t_th = min(THETA_STEPS, Np)
+    t1, t2 = Np // 2 - 1, Np - 1
     bias = bias_slice(0, 1)
+    sel = list(PARITY_PROBLEMS)
     a = G.SquareArray(NX, NY)
     Is = a.current_base(0.0)[:, None, None] * bias[None, :, None]
-    p = G.TimeEvolutionProblem(a, time_step=DT, time_step_count=Nt, current_sources=Is, external_flux=FRUST,
-                               store_time_steps=[t1, t2], store_voltage=False, store_current=False)
-    th_g = p.compute().get_theta()[:, list(PARITY_PROBLEMS), :]
-    sel = np.asarray(bias)[list(PARITY_PROBLEMS)]
-    po = G.TimeEvolutionProblem(a, time_step=DT, time_step_count=Nt,
-                                current_sources=a.current_base(0.0)[:, None, None] * sel[None, :, None],
-                                external_flux=FRUST, store_time_steps=[t1, t2], store_voltage=False,
-                                store_current=False)
+
+    def gpu_theta(Nt, store):
+        p = G.TimeEvolutionProblem(a, time_step=DT, time_step_count=Nt, current_sources=Is, external_flux=FRUST,
+                                   store_time_steps=store, store_voltage=False, store_current=False)
+        return p.compute().get_theta()[:, sel, :]
+
+    th_g_early = gpu_theta(t_th, [t_th - 1])[:, :, 0]
+    th_g_late = th_e2e[:, sel, :] if th_e2e is not None else gpu_theta(Np, [t1, t2])
     t0 = time.perf_counter()
-    th_o, _, _ = rcsj_oracle.time_evolution(po)
-    t_oracle = time.perf_counter() - t0
+    store = jobs["iv_store"]
+    th_o = np.stack([jobs["iv"][p].get() for p in sel], axis=1)          # (Nj, 6, len(store))
+    th_alt = np.stack([jobs["iv_alt"][p].get()[:, 0] for p in sel], axis=1)
+    t_wait = time.perf_counter() - t0
+    o_early = th_o[:, :, store.index(t_th - 1)]
+    o_late = th_o[:, :, [store.index(t1), store.index(t2)]]
+    scale = np.maximum(1.0, np.abs(o_early).max(0))
+    rel = np.abs(th_g_early - o_early).max(0) / scale
+    rel_self = np.abs(th_alt - o_early).max(0) / scale
     horiz = np.arange(NX * (NY - 1))     # current_base(0) drives the horizontal junctions
     vbar = lambda th: (th[horiz, :, 1] - th[horiz, :, 0]).mean(0) / (DT * (t2 - t1))
-    v_g, v_o = vbar(th_g), vbar(th_o)
+    v_g, v_o = vbar(th_g_late), vbar(o_late)
+    verr = np.abs(v_g - v_o)
+    scale_l = np.maximum(1.0, np.abs(o_late[:, :, 1]).max(0))
+    rel_late = np.abs(th_g_late[:, :, 1] - o_late[:, :, 1]).max(0) / scale_l
     A = a.get_cycle_matrix()
-    vort = lambda th: -(A @ np.round(th[:, :, -1] / (2 * np.pi)))
-    return {"problems": list(PARITY_PROBLEMS), "bias": sel.tolist(), "steps": Nt,
+    vort = lambda th: -(A @ np.round(th / (2 * np.pi)))
+    theta_ok = bool(rel.max() <= 1e-9)
+    vbar_ok = bool(verr.max() <= 1e-6)
+    return {"workload": "W=512 x SquareArray(128,128), f=0.25, bias linspace(0,2,512) x current_base(0), T=0, "
+                        "dt=0.05; all 512 on the GPU, the listed problems in the oracle",
+            "problems": sel, "bias": [float(bias[p]) for p in sel],
+            "theta_step": t_th - 1, "rel_theta_2000": float(rel.max()), "rel_theta_2000_per_problem": rel.tolist(),
+            "theta_tolerance": 1e-9, "theta_within_tolerance": theta_ok,
+            "rel_theta_2000_oracle_vs_oracle": rel_self.tolist(),
+            "oracle_vs_oracle": "the same oracle with SuperLU's MMD(A^T+A) column order instead of COLAMD: "
+                                "the spread FP64 rounding alone causes at this step",
+            "rel_theta_final_per_problem": rel_late.tolist(), "final_step": t2,
             "vbar_window": [t1, t2], "vbar_gpu": v_g.tolist(), "vbar_oracle": v_o.tolist(),
-            "max_abs_vbar_error": float(np.abs(v_g - v_o).max()), "tolerance": 1e-6,
-            "within_tolerance": bool(np.abs(v_g - v_o).max() <= 1e-6),
-            "max_abs_theta_error": float(np.abs(th_g - th_o).max()),
-            "vortex_configurations_equal": bool(np.array_equal(vort(th_g), vort(th_o))),
-            "oracle_seconds": t_oracle,
-            "oracle": "numpy/scipy restatement of the reference loop (pinned to the reference's golden outputs)"}
+            "vbar_10000_max_err": float(verr.max()), "vbar_tolerance": 1e-6, "vbar_within_tolerance": vbar_ok,
+            "within_tolerance": theta_ok and vbar_ok,
+            "vortex_configurations_equal_final": bool(np.array_equal(vort(th_g_late[:, :, 1]), vort(o_late[:, :, 1]))),
+            "vbar_from": "the e2e call's stored steps" if th_e2e is not None else "a separate GPU run",
+            "oracle_wait_seconds": t_wait,
+            "oracle": "numpy/scipy restatement of the reference loop (pinned to the reference's golden outputs), "
+                      "one worker process per problem"}
 
 
 def fp64_peak_tflops(torch):
@@ -494,11 +596,12 @@ def main():
                     help="time steps of the adjoint-cost leg (0 skips it)")
     ap.add_argument("--e2e-steps", type=int, default=10000,
                     help="time steps of the end-to-end compute() call (the workload's 10000)")
-    ap.add_argument("--parity-steps", type=int, default=1000,
-                    help="time steps of the oracle comparison on four of the problems (0 skips it)")
+    ap.add_argument("--parity-steps", type=int, default=10000,
+                    help="time steps of the oracle comparison (the workload's 10000: trajectories after 2000 steps, "
+                         "the IV-curve point from steps 4999 and 9999; 0 skips it)")
     ap.add_argument("--ac-steps", type=int, default=20000, help="steps of the AC-driven 256x256 leg (0 skips it)")
     ap.add_argument("--large-steps", type=int, default=300, help="timed steps of the 1024x1024 leg (0 skips it)")
-    ap.add_argument("--ragged-problems", type=int, default=32,
+    ap.add_argument("--ragged-problems", type=int, default=256,
                     help="problems of the ragged leg, the first of 256 seeded draws (0 skips it)")
     ap.add_argument("--ragged-steps", type=int, default=200, help="timed steps of the ragged leg")
     args = ap.parse_args()
@@ -616,7 +719,8 @@ def main():
         prob1 = make_problem(G, 1, [1.0])
         k1 = max(args.steps, 200)
         plain_ms = {}
-        for mode, tuning in (("pdl", {"pdl": 1}), ("default", None)):
+        for mode, tuning in (("pdl", {"pdl": 1}), ("default", None), ("dataflow", {"schedule": 2}),
+                             ("dataflow_pdl", {"schedule": 2, "pdl": 1})):
             sim1 = GpuSimulation(prob1, tuning=tuning, **factor_opts(args))
             t1 = _timed_steps(torch, sim1, k1)
             plain_ms[mode] = t1 / k1 * 1e3
@@ -625,45 +729,69 @@ def main():
         plain = Nj * k1 / t1
         line["plain_gpu"] = {"value": plain, "unit": "junction-steps/s", "W": 1, "ms_per_step": t1 / k1 * 1e3,
                              "ms_per_step_by_launch_mode": plain_ms, "batched_over_plain": value / world / plain}
-        # end to end through the public API with host buffers
+        # end to end through the public API with host buffers: the workload as a user runs it,
+        # Ne steps with steps Ne/2-1 and Ne-1 stored, the IV-curve point read from them on the
+        # host (config: 10000 steps, the first 5000 discarded). Cold: the first call on an empty
+        # cache (factorisation, plan upload and graph capture inside the timed region); warm:
+        # the same call again (the plan cached; graphs are captured anew per call).
+        th_e2e = None
         if not args.no_e2e:
-            # the workload as a user runs it: Nt steps, steps Nt/2-1 and Nt-1 stored, the IV-curve
-            # point read from them on the host (config: 10000 steps, the first 5000 discarded)
+            from pyjjasim_gb300 import backend as B
+            from pyjjasim_gb300 import plan as P
             Ne = args.e2e_steps
-            make_problem(G, 64, bias).compute(**factor_opts(args))     # warm: plan cache, modules
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            a = G.SquareArray(NX, NY)
-            pe = G.TimeEvolutionProblem(a, time_step=DT, time_step_count=Ne,
-                                        current_sources=a.current_base(0.0)[:, None, None] * bias[None, :, None],
-                                        external_flux=FRUST, store_time_steps=[Ne // 2 - 1, Ne - 1])
-            res = pe.compute(**factor_opts(args))
-            V = res.get_voltage()
-            vbar = (res.get_theta()[:NX * (NY - 1), :, 1] - res.get_theta()[:NX * (NY - 1), :, 0]).mean(0) \
-                / (DT * (Ne - Ne // 2))
-            t_e2e = time.perf_counter() - t0
-            assert np.isfinite(V).all() and np.isfinite(vbar).all()
-            stored = (pe.store_time_steps | np.roll(pe.store_time_steps, -1))  # V needs the previous step
-            h2d = (2 * Nj * W + Nj * W) * 8 + 8           # theta(t-1), theta(t-2), Is (Nj x W), f (scalar)
-            d2h = (int(stored.sum()) + int(pe.store_time_steps.sum())) * Nj * W * 8
+
+            def e2e_call():
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                a = G.SquareArray(NX, NY)
+                pe = G.TimeEvolutionProblem(a, time_step=DT, time_step_count=Ne,
+                                            current_sources=a.current_base(0.0)[:, None, None] * bias[None, :, None],
+                                            external_flux=FRUST, store_time_steps=[Ne // 2 - 1, Ne - 1])
+                res = pe.compute(**factor_opts(args))
+                V = res.get_voltage()
+                th = res.get_theta()
+                vbar = (th[:NX * (NY - 1), :, 1] - th[:NX * (NY - 1), :, 0]).mean(0) / (DT * (Ne - Ne // 2))
+                t = time.perf_counter() - t0
+                assert np.isfinite(V).all() and np.isfinite(vbar).all()
+                return t, th, vbar, dict(B.last_transfer)
+
+            P.clear_cache()
+            t_cold, _, _, _ = e2e_call()
+            t_e2e, th_e2e, vbar, xfer = e2e_call()
             line["e2e"] = {"value": Nj * W * Ne / t_e2e, "unit": "junction-steps/s",
-                           "h2d_bytes_per_step": h2d / Ne, "d2h_bytes_per_step": d2h / Ne,
+                           "h2d_bytes_per_step": xfer["h2d_bytes"] / Ne, "d2h_bytes_per_step": xfer["d2h_bytes"] / Ne,
+                           "bytes_counted": "copies the call made: sources and nonzero initial phases host -> "
+                                            "device, stored phases and currents device -> host",
                            "time_steps_per_call": Ne, "seconds_per_call": t_e2e,
                            "stored_steps": [Ne // 2 - 1, Ne - 1],
                            "iv_curve_vbar_min_max": [float(vbar.min()), float(vbar.max())],
+                           "cold_call": {"value": Nj * W * Ne / t_cold, "seconds_per_call": t_cold,
+                                         "includes": "factorisation, plan upload, graph capture"},
                            "api": "pyjjasim_gb300.TimeEvolutionProblem(...).compute(), inputs built on the "
                                   "host inside the timed region, results (theta, I, V) back on the host"}
+            if Ne != args.parity_steps:
+                th_e2e = None
+        # oracle runs of the parity legs and the ragged batch's current_base solves in spawned
+        # worker processes (started after the e2e timing), overlapping the GPU legs below
+        from oracle import parity_jobs as PJ
+        pool = PJ.pool(min(12, max(1, (os.cpu_count() or 2) - 4)))
+        jobs = start_oracle_jobs(args, pool)
         if args.parity_steps > 0:
-            line["parity"] = parity_leg(G, args.parity_steps)
+            line["parity"] = parity_leg(G, args, jobs, th_e2e)
         # the other configurations of the workload family, each guarded so that one failing
         # leg reports its error instead of losing the line
         others = {}
-        for name, fn in (("ac_driven_256x256", lambda: ac_driven_leg(G, torch, args.ac_steps)),
-                         ("single_1024x1024_w8", lambda: large_array_leg(G, torch, args.large_steps)),
-                         ("ragged", lambda: ragged_leg(G, torch, args.ragged_problems, args.ragged_steps))):
-            if (name.startswith("ac") and args.ac_steps <= 0) or (name.startswith("single") and args.large_steps <= 0) \
-                    or (name == "ragged" and args.ragged_problems <= 0):
-                continue
+        legs = []
+        if args.ac_steps > 0:
+            legs.append(("ac_driven_256x256", lambda: ac_driven_leg(G, torch, args.ac_steps)))
+        if args.large_steps > 0:
+            legs.append(("single_1024x1024_w8", lambda: large_array_leg(
+                G, torch, args.large_steps, jobs["large_base"].get(), jobs.get("large"))))
+        if args.ragged_problems > 0:
+            legs.append(("ragged", lambda: ragged_leg(
+                G, torch, args.ragged_problems, args.ragged_steps,
+                {k: v.get() for k, v in jobs["ragged_bases"].items()})))
+        for name, fn in legs:
             try:
                 others[name] = fn()
             except Exception as e:      # report, keep the headline line
@@ -671,6 +799,8 @@ def main():
             torch.cuda.empty_cache()
         if others:
             line["other_configs"] = others
+        pool.close()
+        pool.join()
         if args.adjoint_steps > 0:
             line["adjoint"] = adjoint_leg(G, torch, args.adjoint_steps)
         if not args.no_cpu_baseline:

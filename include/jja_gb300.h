@@ -5,7 +5,7 @@
  * time_evolution_core(problem, th_store_mask, I_store_mask) (time_evolution.py:461-582),
  * called by time_evolution() (:443) from TimeEvolutionProblem.compute() (:303-307).
  * These entry points replace the pieces of that function; the ctypes binding in
- * pyjjasim_gb300/_native.py (and the stub in INTEGRATION.md) call them.
+ * pyjjasim_gb300/_native.py calls them.
  *
  * Conventions: plain pointers and sizes, no framework types. Functions return 0 on success
  * and a nonzero jja_status otherwise; jja_last_error() gives the message (per thread).
@@ -27,7 +27,7 @@ typedef enum {
   JJA_ERR_ARG = 1,        /* invalid argument / shape */
   JJA_ERR_NOT_SPD = 2,    /* face-space matrix is not positive definite */
   JJA_ERR_CUDA = 3,       /* a CUDA runtime call failed */
-  JJA_ERR_NONFINITE = 4,  /* NaN/Inf detected in the state */
+  JJA_ERR_NONFINITE = 4,  /* a time step produced a NaN or +-inf phase (reported by jja_plan_check) */
   JJA_ERR_INTERNAL = 5
 } jja_status;
 
@@ -139,9 +139,11 @@ int jja_plan_create(const jja_plan_desc* desc, const jja_factor* f, jja_plan** o
 void jja_plan_destroy(jja_plan* p);
 /* Bytes of device memory held by the plan (tables + factor + work vectors). */
 int64_t jja_plan_device_bytes(const jja_plan* p);
-/* Synchronises the device, then reads and clears the plan's device error flag: *flow_timeouts
+/* Synchronises the device, then reads and clears the plan's device error flags: *flow_timeouts
  * = 1 if a wait of a dataflow sweep ran out of its bound since the last call (the results of
- * those steps are invalid), else 0. */
+ * those steps are invalid), else 0. Returns JJA_ERR_NONFINITE when a time step of jja_run /
+ * jja_run_timed produced a NaN or +-inf phase since the last call (a diverging run: NaN or inf
+ * in an input, or a time step too large for the circuit); the state is then invalid. */
 int jja_plan_check(jja_plan* p, int* flow_timeouts);
 /* Test of the bounded waits: runs one forward dataflow sweep whose wait counts can never be
  * reached, then synchronises `stream`. Every wait gives up (the first after its bound, the rest
@@ -260,8 +262,12 @@ int jja_solve(jja_plan* p, const double* b, double* x, void* stream);
  * i.e. Nf * W <= 2,097,152 (for example a 128 x 128 array with W <= 130); larger plans get
  * JJA_ERR_ARG with the limit in the message. The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * The address is looked up again when the device's context was destroyed and created again
+ * (cudaDeviceReset); that call, too, must come before any stream capture.
  * All calls share the array: calls that overlap on the GPU (different streams or threads) race.
- * b and x are caller-owned device arrays (Nf x W, original face order), as for jja_solve. */
+ * b and x are caller-owned device arrays (Nf x W, original face order), as for jja_solve. With a
+ * plan of the dataflow schedule (tuning.schedule = 2) a sweep's bounded wait can run out: the call
+ * still returns 0, so synchronise and call jja_plan_check to confirm the result is valid. */
 int jja_solve_static(jja_plan* p, const double* b, double* x, void* stream);
 
 /* Vortex configurations of n_steps stored phase arrays theta (device, n_steps x Nj x W):

@@ -60,13 +60,16 @@ class NumpyGlobalNoise:
         return self.prev
 
 
-def evolve(problem, th_store_mask, I_store_mask, noise=None, on_step=None):
+def evolve(problem, th_store_mask, I_store_mask, noise=None, on_step=None, factorize=None):
     """Restatement of time_evolution_core (time_evolution.py:461-582).
 
     Returns (th_out, I_out) of shape (Nj, W, sum(mask) + width - 1); slots
     0..width-2 hold the initial conditions (theta and cp(theta)), oldest first.
     ``noise``: callable i -> (Nj, W) standard normals; default NumpyGlobalNoise.
     ``on_step``: optional callable(i) run after step i (used to time the loop).
+    ``factorize``: optional callable K -> solve function replacing the reference's
+    ``scipy.sparse.linalg.factorized`` (a different fill-reducing order of the same LU gives the
+    same algorithm with another rounding: it measures how far rounding alone moves a trajectory).
     """
     c = problem.get_circuit()
     Nj, W, dt = c._Nj(), problem.get_problem_count(), problem._dt()
@@ -94,7 +97,7 @@ def evolve(problem, th_store_mask, I_store_mask, noise=None, on_step=None):
         I_out[:, :, n_init - 1 - lag] = problem._cp(th)
 
     K = A @ (c._L() + scipy.sparse.diags(1.0 / Cnext[:, 0], 0)) @ A.T   # :504-505
-    solve = scipy.sparse.linalg.factorized(K)                          # :506
+    solve = (factorize or scipy.sparse.linalg.factorized)(K)           # :506
     theta_s = np.zeros((Nj, W))
 
     Is, T, Vs, f = problem._Is(0), problem._T(0), problem._Vs(0), problem._f(0)

@@ -15,7 +15,7 @@ The reference ends with a static (Newton) refinement of every problem's final vo
 configuration (``StaticProblem.compute``), which is not part of the time-stepping path built
 here: ``run()`` returns the annealed phases, vortex configurations and temperature profiles,
 and ``compute(static_solver=...)`` hands them to a caller-supplied static solver (for example
-the reference's own, see INTEGRATION).
+the reference's own StaticProblem).
 """
 import ctypes
 from dataclasses import dataclass

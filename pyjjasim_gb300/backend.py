@@ -25,6 +25,9 @@ from . import _native as N
 from . import plan as P
 
 _MAX_OUT_BYTES = 8 << 30   # device bytes for stored steps per segment
+# bytes the last time_evolution_core call copied host -> device (phase history, sources, noise)
+# and device -> host (stored steps), for transfer accounting
+last_transfer = {"h2d_bytes": 0, "d2h_bytes": 0}
 
 
 def _torch():
@@ -157,6 +160,46 @@ class _NumpyNoise:
         return self.prev
 
 
+class HostStage:
+    """Everything the GPU core reads from a problem before its first CUDA call.
+
+    Reads the reference's problem interface (time_evolution.py:93-408): the circuit
+    (``_Nj/_Nf``, and for the plan ``get_cycle_matrix/_Ic/_R/_C/_L``), ``get_problem_count``,
+    ``stencil_width``/``stencil``, ``_dt``/``_Nt``, ``config_at_minus_*`` (the initial phase
+    history, newest first), and per source (Is, f, Vs, T) its per-step getter ``_Is(i)``..., its
+    raw attribute (array or callable) and ``_*_is_timedep``, with the reference's zero test
+    (time_evolution.py:512-519). Works on this package's problem mirror and on the reference's
+    own ``TimeEvolutionProblem`` alike; needs no GPU."""
+
+    SOURCES = (("Is", "_Is", "_Is_is_timedep", "current_sources", "Nj"),
+               ("f", "_f", "_f_is_timedep", "external_flux", "Nf"),
+               ("Vs", "_Vs", "_Vs_is_timedep", "voltage_sources", "Nj"),
+               ("T", "_T", "_T_is_timedep", "temperature", "Nj"))
+
+    def __init__(self, problem):
+        c = problem.get_circuit()
+        if not _is_default_cpr(problem.get_current_phase_relation()):
+            raise NotImplementedError("the GPU core evaluates the default current-phase relation Ic*sin(theta) only")
+        self.problem, self.circuit = problem, c
+        self.Nj, self.Nf, self.W = c._Nj(), c._Nf(), problem.get_problem_count()
+        self.width = problem.stencil_width
+        self.stencil = problem.stencil
+        self.dt, self.Nt = problem._dt(), problem._Nt()
+        hist0 = [problem.config_at_minus_1, problem.config_at_minus_2]
+        if self.width >= 4:
+            hist0.append(problem.config_at_minus_3)
+        if self.width >= 5:
+            hist0.append(problem.config_at_minus_4)
+        shape = (self.Nj, self.W)
+        self.hist0 = [_host_f64(h if np.shape(h) == shape else np.broadcast_to(h, shape)) for h in hist0]
+        self.hist0_zero = [not np.any(h) for h in self.hist0]
+        self.sources = {}
+        for name, getter, timedep, attr, rows in self.SOURCES:
+            get, td, n = getattr(problem, getter), bool(getattr(problem, timedep)), getattr(self, rows)
+            self.sources[name] = dict(getter=get, raw=getattr(problem, attr, None), timedep=td, rows=n,
+                                      zero=_source_is_zero(td, get, n, self.W))
+
+
 class GpuSimulation:
     """Device-resident state of W time-evolution problems of one TimeEvolutionProblem.
 
@@ -172,53 +215,38 @@ class GpuSimulation:
         ``tuning``: launch shape of the triangular solves (plan.TUNING_FIELDS); ``tune=True``
         takes ``relax`` and ``tuning`` from the autotuner (timed once per GPU, circuit and W,
         then cached on disk)."""
+        stage = self.stage = HostStage(problem)       # host reads first: no CUDA call before
         torch = self.torch = _torch()
-        c = problem.get_circuit()
-        if not _is_default_cpr(problem.get_current_phase_relation()):
-            raise NotImplementedError("the GPU core evaluates the default current-phase relation Ic*sin(theta) only")
+        c = stage.circuit
         self.problem = problem
-        self.Nj, self.Nf, self.W = c._Nj(), c._Nf(), problem.get_problem_count()
-        self.width = problem.stencil_width
+        self.Nj, self.Nf, self.W = stage.Nj, stage.Nf, stage.W
+        self.width = stage.width
         self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.h2d_bytes = 0
         with torch.cuda.device(self.dev):
             if tune:
                 from .autotune import autotune
-                opts = autotune(c, problem._dt(), self.W, self.width, nd_leaf=nd_leaf, device=self.dev.index)
+                opts = autotune(c, stage.dt, self.W, self.width, nd_leaf=nd_leaf, device=self.dev.index)
                 ordering, relax, tuning = opts["ordering"], opts["relax"], opts["tuning"]
             self.ordering = P.resolve_ordering(ordering, self.W, self.Nf)
             self.relax, self.tuning = tuple(relax), dict(tuning or {})
             self.stream = stream if stream is not None else torch.cuda.Stream(device=self.dev)
-            self.plan = P.get_plan(c, problem._dt(), self.W, self.width, problem.stencil, nd_leaf=nd_leaf,
+            self.plan = P.get_plan(c, stage.dt, self.W, self.width, stage.stencil, nd_leaf=nd_leaf,
                                    ordering=self.ordering, relax=relax, Ic_w=Ic, tuning=tuning)
-            hist0 = [problem.config_at_minus_1, problem.config_at_minus_2]
-            if self.width >= 4:
-                hist0.append(problem.config_at_minus_3)
-            if self.width >= 5:
-                hist0.append(problem.config_at_minus_4)
-            self.hist0 = hist0
-            self.hist0_zero = []
+            self.hist0, self.hist0_zero = stage.hist0, stage.hist0_zero
             self.hist = []
             with torch.cuda.stream(self.stream):
-                for h in hist0:
-                    h = _host_f64(h if np.shape(h) == (self.Nj, self.W) else np.broadcast_to(h, (self.Nj, self.W)))
-                    zero = not np.any(h)
-                    self.hist0_zero.append(zero)
+                for h, zero in zip(stage.hist0, stage.hist0_zero):
                     if zero:      # the default initial condition: no host->device copy needed
                         self.hist.append(torch.zeros((self.Nj, self.W), dtype=torch.float64, device=self.dev))
                     else:
                         self.hist.append(torch.from_numpy(h).to(self.dev))
                         self.h2d_bytes += h.nbytes
             self.srcs = {}
-            self.Nt = problem._Nt()
-            for name, getter, td, rows, attr in (
-                    ("Is", problem._Is, problem._Is_is_timedep, self.Nj, "current_sources"),
-                    ("f", problem._f, problem._f_is_timedep, self.Nf, "external_flux"),
-                    ("Vs", problem._Vs, problem._Vs_is_timedep, self.Nj, "voltage_sources"),
-                    ("T", problem._T, problem._T_is_timedep, self.Nj, "temperature")):
-                zero = _source_is_zero(td, getter, rows, self.W)
-                self.srcs[name] = _Source(torch, self.dev, self.stream, getter, getattr(problem, attr, None), td,
-                                          rows, self.W, self.Nt, zero)
+            self.Nt = stage.Nt
+            for name, sp in stage.sources.items():
+                self.srcs[name] = _Source(torch, self.dev, self.stream, sp["getter"], sp["raw"], sp["timedep"],
+                                          sp["rows"], self.W, self.Nt, sp["zero"])
             # time-dependent sources share one grid of step windows
             self.windowed = [s for s in self.srcs.values() if s.timedep and not s.zero]
             self.window_K = min((s.K for s in self.windowed), default=0)
@@ -396,6 +424,8 @@ def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", se
     th_idx = np.where(th_store_mask, np.cumsum(th_store_mask) - 1, -1).astype(np.int64)
     I_idx = np.where(I_store_mask, np.cumsum(I_store_mask) - 1, -1).astype(np.int64)
     max_slots = max(1, _MAX_OUT_BYTES // (2 * Nj * W * 8))
+    d2h = 0
+    noise_h2d = 0
     with torch.cuda.device(sim.dev):
         i0 = 0
         while i0 < Nt:
@@ -417,8 +447,13 @@ def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", se
                 torch.from_numpy(th_buf[n_init + base_th:n_init + base_th + cnt_th]).copy_(th_dev)
             if cnt_I:
                 torch.from_numpy(I_buf[n_init + base_I:n_init + base_I + cnt_I]).copy_(I_dev)
+            d2h += (cnt_th + cnt_I) * Nj * W * 8
+            if sim.per_step_host:
+                noise_h2d += (i1 - i0) * Nj * W * 8
             del th_dev, I_dev
             i0 = i1
+    last_transfer["h2d_bytes"] = sim.h2d_bytes + sum(s.h2d_bytes for s in sim.windowed) + noise_h2d
+    last_transfer["d2h_bytes"] = d2h
     return th_buf.transpose(1, 2, 0), I_buf.transpose(1, 2, 0)
 
 

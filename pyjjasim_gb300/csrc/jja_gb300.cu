@@ -162,7 +162,13 @@ struct Tables {
   int face_deg;            // 0 when some face has more than kEllMax junctions (CSR path)
   const int32_t* jf_face;  // 2 per junction: (permuted face << 1) | (A entry is -1), or -1
   const longlong2* sincos; // per k < 65536: {S, C} = {sin, cos}(k pi/32768) in units of 2^-62
+  int* nonfinite;          // set to 1 by k_update when a new phase is NaN or +-inf (read by jja_plan_check)
 };
+
+// NaN or +-inf: all exponent bits set (an integer test, no FP64 instruction)
+__device__ __forceinline__ bool non_finite(double v) {
+  return ((unsigned)__double2hiint(v) & 0x7ff00000u) == 0x7ff00000u;
+}
 
 // +-v by flipping the sign bit (no FP64 instruction)
 __device__ __forceinline__ double signed_by(double v, int neg) {
@@ -504,6 +510,7 @@ __global__ void __launch_bounds__(256, JJA_UPDATE_MIN_BLOCKS) k_update(StepArgs 
     double y = p0 >= 0 ? signed_by(J[(int64_t)(p0 >> 1) * a.W + w], p0 & 1) : 0.0;
     if (p1 >= 0) y += signed_by(J[(int64_t)(p1 >> 1) * a.W + w], p1 & 1);
     const double th = fma(y, __ldg(t.inv_c0 + j), -q[e]);
+    if (non_finite(th)) *t.nonfinite = 1;   // a diverging run is reported, not silently continued
     double hist[4];
     if (kFuseNext) {
       hist[0] = th;
@@ -1343,7 +1350,7 @@ struct jja_plan {
   };
   std::vector<CachedGraph> graphs;
   std::vector<CachedGraph> adj_graphs;   // adjoint segment walks
-  static constexpr size_t kMaxGraphs = 8;
+  static constexpr size_t kMaxGraphs = 16;   // 5 graph lengths x two alternating source windows fit
   ~jja_plan() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
     for (auto& g : adj_graphs) cudaGraphExecDestroy(g.exec);
@@ -1872,8 +1879,10 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
       p->b_notify = p->up(S.bnot.data(), S.bnot.size());
       p->counters = p->up<unsigned>(nullptr, 2 * ((size_t)ns + 1));
       JJA_CUDA(cudaMemset(p->counters, 0, 2 * ((size_t)ns + 1) * sizeof(unsigned)));
-      p->flow_err = p->up<int>(nullptr, 1);
-      JJA_CUDA(cudaMemset(p->flow_err, 0, sizeof(int)));
+      // device error flags: [0] a dataflow wait ran out, [1] a non-finite phase was produced
+      p->flow_err = p->up<int>(nullptr, 2);
+      JJA_CUDA(cudaMemset(p->flow_err, 0, 2 * sizeof(int)));
+      p->t.nonfinite = p->flow_err + 1;
       int dev = 0, nsm = 0;
       JJA_CUDA(cudaGetDevice(&dev));
       JJA_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -1930,10 +1939,14 @@ int jja_plan_check(jja_plan* p, int* flow_timeouts) {
   return guarded([&] {
     if (!p || !flow_timeouts) throw Error(JJA_ERR_ARG, "jja_plan_check: null argument");
     JJA_CUDA(cudaDeviceSynchronize());
-    int h = 0;
-    JJA_CUDA(cudaMemcpy(&h, p->flow_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (h) JJA_CUDA(cudaMemset(p->flow_err, 0, sizeof(int)));
-    *flow_timeouts = h;
+    int h[2] = {0, 0};
+    JJA_CUDA(cudaMemcpy(h, p->flow_err, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+    if (h[0] || h[1]) JJA_CUDA(cudaMemset(p->flow_err, 0, 2 * sizeof(int)));
+    *flow_timeouts = h[0];
+    if (h[1])
+      throw Error(JJA_ERR_NONFINITE, "jja_plan_check: a time step produced a non-finite phase (NaN or inf) since the "
+                                     "last check; the state and the outputs of those steps are invalid (check the "
+                                     "inputs for NaN/inf, or a time step too large for the circuit)");
   });
 }
 
@@ -1967,19 +1980,53 @@ __device__ __align__(256) double g_static_scratch[kStaticScratchDoubles];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_static_mutex;
-double* g_static_ptr[kMaxDevices] = {};
+// the array's device address per device, and the CUDA context it was looked up in: a context
+// that was destroyed and created again (cudaDeviceReset, a framework tearing down its primary
+// context) loads the module anew, so the address is looked up again for a new context
+struct StaticScratchSlot {
+  void* ctx = nullptr;
+  double* ptr = nullptr;
+};
+StaticScratchSlot g_static_slot[kMaxDevices];
 
-double* static_scratch_for_current_device() {
+// the calling thread's current CUDA context (driver entry point cuCtxGetCurrent, fetched through
+// the runtime so the library needs no link-time dependency on the driver library)
+void* current_context() {
+  using CtxGetCurrent = int (*)(void**);
+  static CtxGetCurrent fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<CtxGetCurrent>(f);
+  }();
+  if (!fn) throw Error(JJA_ERR_CUDA, "jja_solve_static: the driver entry point cuCtxGetCurrent is unavailable");
+  void* ctx = nullptr;
+  if (fn(&ctx) != 0 || !ctx) throw Error(JJA_ERR_CUDA, "jja_solve_static: no current CUDA context");
+  return ctx;
+}
+
+double* static_scratch_for_current_device(cudaStream_t st) {
   int dev = 0;
   JJA_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) throw Error(JJA_ERR_ARG, "jja_solve_static: device index out of range");
+  // a runtime call on the stream first: it binds the device's context to this thread
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  JJA_CUDA(cudaStreamIsCapturing(st, &cap));
+  void* ctx = current_context();
   std::lock_guard<std::mutex> lock(g_static_mutex);
-  if (!g_static_ptr[dev]) {
+  StaticScratchSlot& slot = g_static_slot[dev];
+  if (slot.ctx != ctx || !slot.ptr) {
+    if (cap != cudaStreamCaptureStatusNone)
+      throw Error(JJA_ERR_ARG, "jja_solve_static: the first call on a device (or after its context was re-created) "
+                               "must come before any stream capture");
     void* ptr = nullptr;
     JJA_CUDA(cudaGetSymbolAddress(&ptr, g_static_scratch));
-    g_static_ptr[dev] = static_cast<double*>(ptr);
+    slot.ctx = ctx;
+    slot.ptr = static_cast<double*>(ptr);
   }
-  return g_static_ptr[dev];
+  return slot.ptr;
 }
 
 // the level sweeps of launch_levels with explicit work vectors
@@ -2000,9 +2047,9 @@ int jja_solve_static(jja_plan* p, const double* b, double* x, void* stream) {
       throw Error(JJA_ERR_ARG, "jja_solve_static: faces x problems = " + std::to_string(NfW) +
                                    " exceeds the static scratch limit of " +
                                    std::to_string(kStaticScratchDoubles / 2) + " (32 MiB for two work vectors)");
-    double* bx = static_scratch_for_current_device();   // permuted right-hand side, later the solution
-    double* z = bx + NfW;                              // forward-substitution result
     cudaStream_t st = (cudaStream_t)stream;
+    double* bx = static_scratch_for_current_device(st);   // permuted right-hand side, later the solution
+    double* z = bx + NfW;                                // forward-substitution result
     // every element of both work vectors is written before it is read: nothing to clear
     k_permute_rows<<<grid_for(NfW, 256), 256, 0, st>>>(b, bx, p->perm, p->Nf, p->W, 1);
     g_launches++;
@@ -2185,23 +2232,31 @@ int jja_run(jja_plan* p, jja_state* s, int nsteps, const int64_t* th_slot, const
     }
     join_groups(p, st);
     const int period = p->width - 1;  // history rotation period
-    const int G = 16 * period;        // steps per captured graph: pointers return to their places
     int i = 0;
     while (i < nsteps) {
       // a run of steps that store nothing (or, with store_all, whose slots the device derives
-      // from the step counter) can be replayed from a captured graph; the call's last step
-      // stays out of it (it runs unfused: the look-ahead q it would evaluate belongs to a step
+      // from the step counter) can be replayed from captured graphs; the call's last step
+      // stays out of them (it runs unfused: the look-ahead q it would evaluate belongs to a step
       // outside this call, whose sources may lie outside the source window)
       int run = 0;
       while (i + run < nsteps && (!th_slot || th_slot[i + run] < 0) && (!I_slot || I_slot[i + run] < 0)) ++run;
       const int graphable = (i + run == nsteps) ? run - 1 : run;
-      // capture needs a non-default stream; the per-step noise buffer is refilled by the host
-      if (use_graph && st != nullptr && graphable >= G && s->noise_mode != JJA_NOISE_BUFFER) {
-        cudaGraphExec_t exec = graph_for(p, s, st, G);
-        const int reps = graphable / G;
-        for (int r = 0; r < reps; ++r) JJA_CUDA(cudaGraphLaunch(exec, st));
-        i += reps * G;
-        run -= reps * G;
+      // capture needs a non-default stream; the per-step noise buffer is refilled by the host.
+      // Graphs hold 16, 8, 4, 2 or 1 rotation periods of steps (pointers return to their places
+      // after each), taken greedily, so short runs replay graphs too and at most one period of
+      // steps runs eagerly
+      if (use_graph && st != nullptr && graphable >= period && s->noise_mode != JJA_NOISE_BUFFER) {
+        int done = 0;
+        for (int mult = 16; mult >= 1; mult >>= 1) {
+          const int G = mult * period;
+          if (graphable - done < G) continue;
+          cudaGraphExec_t exec = graph_for(p, s, st, G);
+          const int reps = (graphable - done) / G;
+          for (int r = 0; r < reps; ++r) JJA_CUDA(cudaGraphLaunch(exec, st));
+          done += reps * G;
+        }
+        i += done;
+        run -= done;
       }
       const int eager = (i < nsteps) ? std::max(run, 1) : 0;
       if (eager > 0 && i < nsteps) {

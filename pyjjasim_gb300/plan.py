@@ -10,6 +10,7 @@ pay the factorisation once.
 """
 import ctypes
 import hashlib
+import threading
 from collections import OrderedDict
 
 import numpy as np
@@ -21,6 +22,8 @@ _FACTORS = OrderedDict()
 _PLANS = OrderedDict()
 MAX_FACTORS = 4
 MAX_PLANS = 4
+_CACHE_LOCK = threading.Lock()   # the caches are shared by host threads (ragged parts build in parallel);
+                                 # the lock covers lookups and insertions, not the factorisations
 
 # Extrapolation weights of the CPR argument on theta(t-1), theta(t-2), ... (time_evolution.py:547-553)
 EXTRAP = {3: (2.0, -1.0), 4: (3.0, -3.0, 1.0), 5: (4.0, -6.0, 4.0, -1.0)}
@@ -223,17 +226,18 @@ def fill_reducing_order(K, ordering, circuit=None):
 def get_factor(circuit, dt, nd_leaf=8, ordering="nd", relax=(-1, -1.0)):
     A, K = face_matrix(circuit, dt)
     key = (_digest(K.indptr, K.indices, K.data), nd_leaf, ordering, tuple(relax))
-    f = _FACTORS.get(key)
-    if f is None:
-        coords, perm = fill_reducing_order(K, ordering, circuit)
-        f = HostFactor(K, coords=coords, perm=perm, nd_leaf=nd_leaf, relax_zeros=relax[0], relax_frac=relax[1])
+    with _CACHE_LOCK:
+        hit = _FACTORS.get(key)
+        if hit is not None:
+            _FACTORS.move_to_end(key)
+            return hit[0], A, key
+    coords, perm = fill_reducing_order(K, ordering, circuit)
+    f = HostFactor(K, coords=coords, perm=perm, nd_leaf=nd_leaf, relax_zeros=relax[0], relax_frac=relax[1])
+    with _CACHE_LOCK:
         _FACTORS[key] = (f, A)
         while len(_FACTORS) > MAX_FACTORS:
             _FACTORS.popitem(last=False)
-    else:
-        _FACTORS.move_to_end(key)
-        f = f[0]
-    return _FACTORS[key][0], A, key
+    return f, A, key
 
 
 def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=8, ordering="auto", relax=(-1, -1.0), Ic_w=None,
@@ -249,17 +253,20 @@ def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=8, ordering="auto",
     ic = np.asarray(circuit._Ic(), np.float64) if Ic_w is None else Ic_w
     tkey = tuple(int((tuning or {}).get(f, 0)) for f in TUNING_FIELDS)
     key = (fkey, W, stencil_width, Ic_w is None, tkey, _digest(ic, *coef, Rv, A.indptr, A.indices, A.data))
-    p = _PLANS.get(key)
-    if p is None:
-        p = DevicePlan(circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=Ic_w, tuning=tuning)
+    with _CACHE_LOCK:
+        p = _PLANS.get(key)
+        if p is not None:
+            _PLANS.move_to_end(key)
+            return p
+    p = DevicePlan(circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=Ic_w, tuning=tuning)
+    with _CACHE_LOCK:
         _PLANS[key] = p
         while len(_PLANS) > MAX_PLANS:
             _PLANS.popitem(last=False)
-    else:
-        _PLANS.move_to_end(key)
     return p
 
 
 def clear_cache():
-    _PLANS.clear()
-    _FACTORS.clear()
+    with _CACHE_LOCK:
+        _PLANS.clear()
+        _FACTORS.clear()

@@ -1,13 +1,13 @@
 """Generate the golden fixtures under tests/golden/ by running the reference pyjjasim.
 
 This script is the only committed code that imports the reference package. It runs
-in a container that has the reference sources mounted at /root/reference (read-only);
+where the reference sources are present (read-only; their directory is given by --ref);
 the fixtures it writes (`*.npz`) are what the tests read on machines without it.
 
 Import recipe: the reference imports itself as ``pyjjasim.*`` (pyjjasim/__init__.py),
 imports matplotlib at module load (embedded_graph.py:3-4, circuit_visualize.py:3-11),
 and calls ``np.asscalar`` (time_evolution.py:322), which numpy removed. So the script
-puts a symlink ``pyjjasim -> /root/reference`` in a temporary directory on sys.path,
+puts a symlink ``pyjjasim -> <ref>`` in a temporary directory on sys.path,
 stubs the matplotlib modules and re-adds ``np.asscalar``. Nothing in the reference is
 modified; bytecode writing is disabled so its read-only tree is never touched.
 
@@ -17,7 +17,7 @@ the parameters of a source callable, seeds, store masks) and the reference outpu
 derived observables: node phases and potentials, cycle currents, flux, supercurrent and the
 energies), so a test can rebuild the same problem with no reference present.
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+Usage:  python tests/golden/make_golden.py --ref <reference source directory>
 """
 import argparse
 import os
@@ -32,12 +32,23 @@ import scipy.sparse
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
+MATPLOTLIB_STUBS = ["matplotlib", "matplotlib.pyplot", "matplotlib.collections", "matplotlib.animation",
+                    "matplotlib.colors", "matplotlib.cm", "matplotlib.patches", "matplotlib.lines",
+                    "matplotlib.legend_handler", "matplotlib.text"]
+
+
+def _stub_attr(name):
+    # module metadata (__file__, __path__, ...) stays absent, so tools that walk sys.modules
+    # (inspect) see an ordinary module; every other name is a no-op callable
+    if name.startswith("__"):
+        raise AttributeError(name)
+    return lambda *a, **k: None
+
+
 def import_reference(ref_dir):
-    for m in ["matplotlib", "matplotlib.pyplot", "matplotlib.collections", "matplotlib.animation",
-              "matplotlib.colors", "matplotlib.cm", "matplotlib.patches", "matplotlib.lines",
-              "matplotlib.legend_handler", "matplotlib.text"]:
+    for m in MATPLOTLIB_STUBS:
         mod = types.ModuleType(m)
-        mod.__getattr__ = lambda name: (lambda *a, **k: None)
+        mod.__getattr__ = _stub_attr
         sys.modules[m] = mod
     if not hasattr(np, "asscalar"):
         np.asscalar = lambda a: a.item()
@@ -148,7 +159,7 @@ def every(Nt, k):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="directory of the reference pyjjasim sources")
     ap.add_argument("--anneal-only", action="store_true", help="write only the AnnealingProblem fixtures")
     args = ap.parse_args()
     pj = import_reference(args.ref)
