@@ -460,7 +460,10 @@ def parity_leg(G, args, jobs, th_e2e=None):
             "vbar_window": [t1, t2], "vbar_gpu": v_g.tolist(), "vbar_oracle": v_o.tolist(),
             "vbar_10000_max_err": float(verr.max()), "vbar_tolerance": 1e-6, "vbar_within_tolerance": vbar_ok,
             "within_tolerance": theta_ok and vbar_ok,
-            "vortex_configurations_equal_final": bool(np.array_equal(vort(th_g_late[:, :, 1]), vort(o_late[:, :, 1]))),
+            "vortex_configurations_equal_2000": bool(np.array_equal(vort(th_g_early), vort(o_early))),
+            "vortex_faces_differing_final": int(np.sum(vort(th_g_late[:, :, 1]) != vort(o_late[:, :, 1]))),
+            "final_step_note": "by the last step the running states have moved apart chaotically (relative theta "
+                               "errors above); the time-averaged voltage agrees within its tolerance",
             "vbar_from": "the e2e call's stored steps" if th_e2e is not None else "a separate GPU run",
             "oracle_wait_seconds": t_wait,
             "oracle": "numpy/scipy restatement of the reference loop (pinned to the reference's golden outputs), "

@@ -270,6 +270,75 @@ int jja_solve(jja_plan* p, const double* b, double* x, void* stream);
  * still returns 0, so synchronise and call jja_plan_check to confirm the result is valid. */
 int jja_solve_static(jja_plan* p, const double* b, double* x, void* stream);
 
+/* -------------------------------------------------------------------- static problems --- */
+/* The reference's static (stationary) problem solver on the GPU: the Newton iteration
+ * static_compute (static_problem.py:1400-1515) and the London approximation
+ * london_approximation (:1378-1395), for W problems on one circuit at once. Every Newton
+ * iteration refactors A (L + diag(1/q)) A^T, q = Ic cos(theta), numerically on the device
+ * (supernodal LDL^T on the symbolic structure of `factor`, which must have the sparsity pattern
+ * of A (L + D) A^T for a diagonal D, e.g. the factor of A (L + I) A^T), and solves with it.
+ * Vectors are problem-major device arrays: (W x Nj) per junction, (W x Nf) per face (original
+ * face order), element (w, j) at w*Nj + j. */
+typedef struct jja_static jja_static;
+
+typedef struct {
+  int Nj, Nf, Nn, W;          /* junctions, faces, nodes, problems */
+  const int64_t* a_rowptr;    /* cycle matrix A (Nf x Nj, entries +-1), CSR over the original face order */
+  const int32_t* a_col;
+  const double* a_val;
+  const int64_t* m_rowptr;    /* cut matrix M (Nn x Nj), CSR (Kirchhoff residual) */
+  const int32_t* m_col;
+  const double* m_val;
+  const int64_t* l_rowptr;    /* inductance L (Nj x Nj), CSR; all NULL when the circuit has none */
+  const int32_t* l_col;
+  const double* l_val;
+  const int64_t* kl_colptr;   /* A L A^T (Nf x Nf, both triangles, CSC over the original face order); NULL: none */
+  const int32_t* kl_rowind;
+  const double* kl_val;
+  const double* Ic;           /* critical currents (Nj) */
+  double A_norm, M_norm;      /* ||A||_2 and ||M||_2 (sqrt of the largest eigenvalue of A A^T, M M^T),
+                                 the normalisers of the reference's residuals (josephson_circuit.py:762-780) */
+} jja_static_desc;
+
+int jja_static_create(const jja_static_desc* desc, const jja_factor* factor, jja_static** out);
+void jja_static_destroy(jja_static* sp);
+int64_t jja_static_device_bytes(const jja_static* sp);
+
+/* Diagnostic of the device factorisation: x_w = (A (L + diag(iq_w)) A^T)^-1 b_w for every problem
+ * (iq: device W x Nj, b, x: device W x Nf). pivot_errors (host, W entries, or NULL) receives 1 for a
+ * problem whose elimination met a zero or non-finite pivot (the matrix may be indefinite; the
+ * elimination does not pivot). */
+int jja_static_solve(jja_static* sp, const double* iq, const double* b, double* x, int* pivot_errors, void* stream);
+
+/* London approximation in phase zone n (static_problem.py:1378-1395):
+ * theta = iIc (A^T (A (iIc + L) A^T)^-1 (2 pi (n - f) - A (iIc + L) Is) + Is), iIc = 1/Ic (0 where
+ * |Ic| <= 1e-12). Is, theta: device W x Nj; f: device W x Nf; n: device W x Nf int32. */
+int jja_static_london(jja_static* sp, const double* Is, const double* f, const int32_t* n, double* theta,
+                      void* stream);
+
+typedef struct {
+  double* theta;              /* device W x Nj: initial guess in, solution out */
+  const double* Is;           /* device W x Nj current sources */
+  const double* f;            /* device W x Nf external flux (phase zone z = 0, as StaticProblem.compute uses) */
+  const int32_t* n;           /* device W x Nf target vortex configuration */
+  double tol;                 /* residual tolerance (the reference's default 1e-10) */
+  int maxiter;                /* iteration limit (default 30) */
+  int stop_as_residual_increases;   /* stop when error(iter) > error(iter - 3) (default 1) */
+  int stop_if_not_target_n;         /* the reference's flag, with its behaviour (default 0) */
+} jja_newton_args;
+
+typedef struct {               /* host arrays the caller provides */
+  int* status;                /* W: 0 converged on the target configuration, 1 diverged, +2 at maxiter */
+  int* iterations;            /* W: Newton steps taken */
+  double* residuals;          /* W x (maxiter + 1): max(Kirchhoff, winding) residual per iterate (0 past the last) */
+  int* is_target;             /* W x (maxiter + 1): 1 where the iterate has the target vortex configuration */
+} jja_newton_result;
+
+/* static_compute for every problem: the stop rules, residuals and status of the reference's
+ * Newton iteration (static_problem.py:1476-1515, NewtonIterInfo :88-201); every problem stops on
+ * its own. The reference's NaN rule is kept (theta += 1e10 when the solve is not finite). */
+int jja_static_newton(jja_static* sp, const jja_newton_args* args, jja_newton_result* result, void* stream);
+
 /* Vortex configurations of n_steps stored phase arrays theta (device, n_steps x Nj x W):
  * n_s(f, w) = -sum_j A_fj round(theta_s(j, w) / 2 pi) (TimeEvolutionResult.get_vortex_configuration,
  * time_evolution.py:734-755), written to n_out (device n_steps x Nf x W int32, original face

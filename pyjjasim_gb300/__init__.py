@@ -20,10 +20,12 @@ Drop-in replacement of the reference's RCSJ time-stepping hot path
 from .circuit import Circuit, HoneycombArray, SquareArray, TriangularArray
 from .problem import (CurrentNotStored, DataAtTimepointNotStored, DefaultCPR, ThetaNotStored, TimeEvolutionProblem,
                       TimeEvolutionResult, VoltageNotStored, time_evolution)
+from .static import NewtonIterInfo, StaticConfiguration, StaticProblem
 
 __all__ = ["Circuit", "SquareArray", "HoneycombArray", "TriangularArray", "DefaultCPR", "TimeEvolutionProblem",
            "TimeEvolutionResult", "time_evolution", "install", "uninstall", "time_evolution_core",
-           "ThetaNotStored", "CurrentNotStored", "VoltageNotStored", "DataAtTimepointNotStored"]
+           "ThetaNotStored", "CurrentNotStored", "VoltageNotStored", "DataAtTimepointNotStored",
+           "StaticProblem", "StaticConfiguration", "NewtonIterInfo"]
 
 
 def time_evolution_core(problem, th_store_mask, I_store_mask, **options):

@@ -64,6 +64,25 @@ class AdjointSegmentArgs(ctypes.Structure):
                 ("usum", c_void_p), ("musum", c_void_p), ("gIc", c_void_p), ("use_graph", c_int)]
 
 
+class StaticDesc(ctypes.Structure):
+    _fields_ = [("Nj", c_int), ("Nf", c_int), ("Nn", c_int), ("W", c_int),
+                ("a_rowptr", P_i64), ("a_col", P_i32), ("a_val", P_f64),
+                ("m_rowptr", P_i64), ("m_col", P_i32), ("m_val", P_f64),
+                ("l_rowptr", P_i64), ("l_col", P_i32), ("l_val", P_f64),
+                ("kl_colptr", P_i64), ("kl_rowind", P_i32), ("kl_val", P_f64),
+                ("Ic", P_f64), ("A_norm", c_double), ("M_norm", c_double)]
+
+
+class NewtonArgs(ctypes.Structure):
+    _fields_ = [("theta", c_void_p), ("Is", c_void_p), ("f", c_void_p), ("n", c_void_p), ("tol", c_double),
+                ("maxiter", c_int), ("stop_as_residual_increases", c_int), ("stop_if_not_target_n", c_int)]
+
+
+class NewtonResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.POINTER(c_int)), ("iterations", ctypes.POINTER(c_int)), ("residuals", P_f64),
+                ("is_target", ctypes.POINTER(c_int))]
+
+
 # exported symbol -> (restype, argtypes); every symbol of include/jja_gb300.h
 SIGNATURES = {
     "jja_factor_create": (c_int, [c_int, P_i64, P_i32, P_f64, P_f64, P_f64, P_i32, ctypes.POINTER(FactorOpts),
@@ -86,6 +105,12 @@ SIGNATURES = {
     "jja_adjoint_step": (c_int, [c_void_p, ctypes.POINTER(AdjointArgs), c_void_p]),
     "jja_adjoint_segment": (c_int, [c_void_p, ctypes.POINTER(AdjointSegmentArgs), c_void_p]),
     "jja_adjoint_flux": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "jja_static_create": (c_int, [ctypes.POINTER(StaticDesc), c_void_p, ctypes.POINTER(c_void_p)]),
+    "jja_static_destroy": (None, [c_void_p]),
+    "jja_static_device_bytes": (c_int64, [c_void_p]),
+    "jja_static_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, ctypes.POINTER(c_int), c_void_p]),
+    "jja_static_london": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "jja_static_newton": (c_int, [c_void_p, ctypes.POINTER(NewtonArgs), ctypes.POINTER(NewtonResult), c_void_p]),
     "jja_vortex": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "jja_eval_sin": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
     "jja_sin_host": (c_int, [P_f64, P_f64, P_f64, c_int64]),

@@ -12,10 +12,11 @@ config_at_minus_1 = config_at_minus_2 = the last phase; the mobility divides by
 Nf dt (interval_count - 1); five closing runs at T = 0 with half the time step.
 
 The reference ends with a static (Newton) refinement of every problem's final vortex
-configuration (``StaticProblem.compute``), which is not part of the time-stepping path built
-here: ``run()`` returns the annealed phases, vortex configurations and temperature profiles,
-and ``compute(static_solver=...)`` hands them to a caller-supplied static solver (for example
-the reference's own StaticProblem).
+configuration (``StaticProblem.compute`` of ``get_static_problem(n_p, problem_nr=0)``,
+time_evolution.py:1187-1190). ``compute()`` does the same on the GPU, all problems in one
+batched Newton iteration (``static.compute_many``), and returns the reference's triple
+(status, configurations, temperature profiles); ``run()`` returns the annealed phases, vortex
+configurations, temperature profiles and mobilities without it.
 """
 import ctypes
 from dataclasses import dataclass
@@ -149,17 +150,21 @@ class AnnealingProblem:
                             temperature_profiles=profiles, vortex_mobility=mobility)
 
     def compute(self, static_solver=None, **run_options):
-        """The reference's return value (status, configurations, temperature_profiles) when a
-        ``static_solver(circuit, current_sources, external_flux, vortex_configuration) ->
-        (configuration, status)`` is supplied for the final refinement; without one, raises
-        NotImplementedError (use ``run()``)."""
-        if static_solver is None:
-            raise NotImplementedError("the final static (Newton) refinement is outside the GPU time-stepping "
-                                      "path; call run(), or pass static_solver=...")
+        """The reference's return value (status, configurations, temperature_profiles)
+        (time_evolution.py:1144-1191). The closing static refinement solves every problem's final
+        vortex configuration with the sources and flux of problem 0 (the reference passes
+        problem_nr=0 for all of them) on the GPU; ``static_solver(circuit, current_sources,
+        external_flux, vortex_configuration) -> (configuration, status)`` replaces it."""
         r = self.run(**run_options)
         Nj = self.circuit._Nj()
         Is = np.broadcast_to(np.asarray(self.current_sources, np.float64), (Nj,)) \
             if np.ndim(self.current_sources) <= 1 else np.asarray(self.current_sources)[:, 0, 0]
         f = np.broadcast_to(np.atleast_1d(np.asarray(self.external_flux, np.float64)), (self.circuit._Nf(),))
-        data = [static_solver(self.circuit, Is, f, r.vortex_configuration[:, p]) for p in range(self.problem_count)]
+        if static_solver is not None:
+            data = [static_solver(self.circuit, Is, f, r.vortex_configuration[:, p]) for p in range(self.problem_count)]
+            return np.array([d[1] for d in data]), [d[0] for d in data], r.temperature_profiles
+        from .static import StaticProblem, compute_many
+        problems = [StaticProblem(self.circuit, current_sources=Is.copy(), external_flux=f.copy(),
+                                  vortex_configuration=r.vortex_configuration[:, p]) for p in range(self.problem_count)]
+        data = compute_many(problems)
         return np.array([d[1] for d in data]), [d[0] for d in data], r.temperature_profiles

@@ -27,7 +27,7 @@ def _nvcc():
 
 
 def sources():
-    return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cpp", ".h"))] + \
+    return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cuh", ".cpp", ".h"))] + \
         [os.path.join(ROOT, "include", "jja_gb300.h")]
 
 

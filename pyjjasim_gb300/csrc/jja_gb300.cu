@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <stdexcept>
 #include <string>
 #include <mutex>
@@ -1234,6 +1235,65 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
   return S;
 }
 
+// Face <-> junction tables of a cycle matrix (CSR over the original face order, entries +-1), in
+// the factor's face order: per permuted face its junction codes (junction << 1) | (entry is -1)
+// as CSR (and a fixed-degree copy when every face has at most kEllMax junctions), the original
+// face of each permuted face, and per junction its (at most 2) faces (face << 1) | (entry is -1).
+struct FaceTables {
+  std::vector<int64_t> fj_ptr;
+  std::vector<int32_t> fj_col, face_orig, jf_face, ell;
+  int deg = 0;
+};
+
+FaceTables face_tables(int Nj, int Nf, const int64_t* a_rowptr, const int32_t* a_col, const double* a_val,
+                       const std::vector<int>& perm) {
+  if (Nj >= (1 << 30) || Nf >= (1 << 30)) throw Error(JJA_ERR_ARG, "too many junctions or faces");
+  FaceTables ft;
+  ft.fj_ptr.assign(Nf + 1, 0);
+  ft.face_orig.resize(Nf);
+  ft.jf_face.assign(2 * (size_t)Nj, -1);
+  for (int pn = 0; pn < Nf; ++pn) {
+    const int f = perm[pn];
+    ft.face_orig[pn] = f;
+    for (int64_t q = a_rowptr[f]; q < a_rowptr[f + 1]; ++q) {
+      const int j = a_col[q];
+      const double v = a_val[q];
+      if (j < 0 || j >= Nj) throw Error(JJA_ERR_ARG, "cycle matrix column out of range");
+      if (v != 1.0 && v != -1.0) throw Error(JJA_ERR_ARG, "cycle matrix entries must be +1 or -1");
+      const int neg = v < 0 ? 1 : 0;
+      ft.fj_col.push_back((j << 1) | neg);
+      const int slot = ft.jf_face[2 * (size_t)j] < 0 ? 0 : (ft.jf_face[2 * (size_t)j + 1] < 0 ? 1 : -1);
+      if (slot < 0) throw Error(JJA_ERR_ARG, "a junction lies on more than two faces (non-planar cycle matrix)");
+      ft.jf_face[2 * (size_t)j + slot] = (pn << 1) | neg;
+    }
+    ft.fj_ptr[pn + 1] = (int64_t)ft.fj_col.size();
+  }
+  for (int pn = 0; pn < Nf; ++pn) ft.deg = std::max<int>(ft.deg, (int)(ft.fj_ptr[pn + 1] - ft.fj_ptr[pn]));
+  if (ft.deg >= 1 && ft.deg <= kEllMax) {
+    ft.ell.assign((size_t)Nf * ft.deg, -1);
+    for (int pn = 0; pn < Nf; ++pn)
+      for (int64_t i = ft.fj_ptr[pn]; i < ft.fj_ptr[pn + 1]; ++i)
+        ft.ell[(size_t)pn * ft.deg + (i - ft.fj_ptr[pn])] = ft.fj_col[i];
+  } else {
+    ft.deg = 0;
+  }
+  return ft;
+}
+
+// the face tables into a kernel table set; `up` uploads a host array and returns its device copy
+template <class Up>
+void set_face_tables(Tables& t, const FaceTables& ft, Up up) {
+  t.fj_ptr = up(ft.fj_ptr.data(), ft.fj_ptr.size());
+  t.fj_col = up(ft.fj_col.data(), ft.fj_col.size());
+  if (ft.deg) {
+    t.fj_ell = up(ft.ell.data(), ft.ell.size());
+    t.face_deg = ft.deg;
+  }
+  t.face_orig = up(ft.face_orig.data(), ft.face_orig.size());
+  t.jf_face = up(ft.jf_face.data(), ft.jf_face.size());
+}
+
+
 // Every item of a dataflow sweep may only wait for items that come before it in the sweep's
 // order, and the counts it waits for must be exactly the number of items that will count.
 // Otherwise warps could wait for items no running warp holds.
@@ -1735,27 +1795,7 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->rows_per_lane_fwd = rows_per_lane_of(tu, true, d->W);
     p->pdl = tu.pdl == 1;
     const int Nj = d->Nj, Nf = d->Nf;
-    // face -> junction entries in the factor's face order; junction -> (<= 2) faces
-    std::vector<int64_t> fj_ptr(Nf + 1, 0);
-    std::vector<int32_t> fj_col;                 // (junction << 1) | (entry is -1)
-    std::vector<int32_t> face_orig(Nf), jf_face(2 * (size_t)Nj, -1);   // (face << 1) | (entry is -1)
-    for (int pn = 0; pn < Nf; ++pn) {
-      const int f = F.perm[pn];
-      face_orig[pn] = f;
-      for (int64_t q = d->a_rowptr[f]; q < d->a_rowptr[f + 1]; ++q) {
-        const int j = d->a_col[q];
-        const double v = d->a_val[q];
-        if (j < 0 || j >= Nj) throw Error(JJA_ERR_ARG, "cycle matrix column out of range");
-        if (v != 1.0 && v != -1.0) throw Error(JJA_ERR_ARG, "cycle matrix entries must be +1 or -1");
-        if (Nj >= (1 << 30) || Nf >= (1 << 30)) throw Error(JJA_ERR_ARG, "too many junctions or faces");
-        const int neg = v < 0 ? 1 : 0;
-        fj_col.push_back((j << 1) | neg);
-        int slot = jf_face[2 * (size_t)j] < 0 ? 0 : (jf_face[2 * (size_t)j + 1] < 0 ? 1 : -1);
-        if (slot < 0) throw Error(JJA_ERR_ARG, "a junction lies on more than two faces (non-planar cycle matrix)");
-        jf_face[2 * (size_t)j + slot] = (pn << 1) | neg;
-      }
-      fj_ptr[pn + 1] = (int64_t)fj_col.size();
-    }
+    const FaceTables ft = face_tables(Nj, Nf, d->a_rowptr, d->a_col, d->a_val, F.perm);
     {
       // coefficients multiplied by 1/c0 once on the host (the junction kernels then need no
       // final multiply). "resistive": width 3 and c2 = Cv = 0 everywhere, in which case
@@ -1788,21 +1828,7 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
       p->t.Rvq = p->up(rvq.data(), rvq.size());
     }
     p->t.inv_c0 = p->up(d->inv_c0, Nj);
-    p->t.fj_ptr = p->up(fj_ptr.data(), fj_ptr.size());
-    p->t.fj_col = p->up(fj_col.data(), fj_col.size());
-    {
-      int deg = 0;
-      for (int pn = 0; pn < Nf; ++pn) deg = std::max<int>(deg, (int)(fj_ptr[pn + 1] - fj_ptr[pn]));
-      if (deg >= 1 && deg <= kEllMax) {
-        std::vector<int32_t> ell((size_t)Nf * deg, -1);
-        for (int pn = 0; pn < Nf; ++pn)
-          for (int64_t i = fj_ptr[pn]; i < fj_ptr[pn + 1]; ++i) ell[(size_t)pn * deg + (i - fj_ptr[pn])] = fj_col[i];
-        p->t.fj_ell = p->up(ell.data(), ell.size());
-        p->t.face_deg = deg;
-      }
-    }
-    p->t.face_orig = p->up(face_orig.data(), face_orig.size());
-    p->t.jf_face = p->up(jf_face.data(), jf_face.size());
+    set_face_tables(p->t, ft, [&](auto* h, size_t n) { return p->up(h, n); });
     p->perm = p->up(F.perm.data(), F.perm.size());
     {
       const std::vector<longlong2> tab = build_sin_table();
@@ -2350,3 +2376,4 @@ int jja_run_timed(jja_plan* p, jja_state* s, int nsteps, double* stage_ms, void*
 }
 
 }  // extern "C"
+#include "jja_static.cuh"

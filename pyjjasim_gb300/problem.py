@@ -117,6 +117,15 @@ class TimeEvolutionProblem:
     def get_current_phase_relation(self):
         return self.current_phase_relation
 
+    def get_static_problem(self, vortex_configuration, problem_nr=0, time_step=0):
+        """A StaticProblem with this problem's sources and flux of one problem at one step
+        (time_evolution.py:151-172); it computes on the GPU."""
+        from .static import StaticProblem
+        return StaticProblem(self.circuit, current_sources=self._Is(time_step)[:, problem_nr].copy(),
+                             external_flux=self._f(time_step)[:, problem_nr].copy(),
+                             vortex_configuration=vortex_configuration,
+                             current_phase_relation=self.current_phase_relation)
+
     def get_external_flux(self):
         return self.external_flux
 

@@ -142,7 +142,8 @@ def anneal_case(pj, name, circuit, seed, **params):
         pj.TimeEvolutionProblem.get_static_problem = orig
     d = circuit_parts(circuit)
     d.update(seed=np.int64(seed), temperature_profiles=profiles, status=np.asarray(status),
-             final_vortex=np.stack(handed, axis=1))
+             final_vortex=np.stack(handed, axis=1),
+             static_theta=np.stack([cfg.get_theta() for cfg in configs], axis=1))
     for k, v in params.items():
         d["param_" + k] = np.asarray(v)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
@@ -161,9 +162,14 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", required=True, help="directory of the reference pyjjasim sources")
     ap.add_argument("--anneal-only", action="store_true", help="write only the AnnealingProblem fixtures")
+    ap.add_argument("--static-only", action="store_true",
+                    help="write only the StaticProblem and AnnealingProblem fixtures")
     args = ap.parse_args()
     pj = import_reference(args.ref)
     if args.anneal_only:
+        return anneal_fixtures(pj)
+    if args.static_only:
+        static_fixtures(pj)
         return anneal_fixtures(pj)
 
     # Lattice fixtures: cycle matrices, cut matrices and current_base for the three lattice kinds.
@@ -259,6 +265,57 @@ def main():
     run_case(pj, "c10_square7x5_timedep", a, 0.1, Nt, f=fa, Is=Is[:, None, None], T=Ta, seed=9,
              store=every(Nt, 3), th_m1=th1, th_m2=th2)
     anneal_fixtures(pj)
+
+
+def static_case(pj, name, circuit, Is, f, n, initial_guess=None, **kw):
+    """Run the reference's StaticProblem(...).compute() (the Newton iteration static_compute,
+    static_problem.py:1400-1515, started from approximate() unless a guess is given) and save its
+    inputs, the initial guess, the solution, the status and the iteration record."""
+    prob = pj.StaticProblem(circuit, current_sources=Is, external_flux=f, vortex_configuration=n)
+    theta0 = prob.approximate().get_theta() if initial_guess is None else np.asarray(initial_guess, np.float64)
+    config, status, info = prob.compute(initial_guess=initial_guess, **kw)
+    d = circuit_parts(circuit)
+    d.update(in_Is=np.broadcast_to(np.asarray(Is, np.float64), (circuit.junction_count(),)).copy(),
+             in_f=np.broadcast_to(np.asarray(f, np.float64), (circuit.face_count(),)).copy(),
+             in_n=np.broadcast_to(np.asarray(n, np.int64), (circuit.face_count(),)).copy(),
+             theta0=np.asarray(theta0, np.float64), guess_given=np.int64(initial_guess is not None),
+             theta=config.get_theta().copy(), current=config.get_current().copy(),
+             vortex=config.get_vortex_configuration().astype(np.int64), status=np.int64(status),
+             iterations=np.int64(info.get_number_of_iterations()), residuals=info.get_residual().copy(),
+             is_target=info.get_is_target_vortex_configuration().astype(np.int64))
+    for k, v in kw.items():
+        d["param_" + k] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+    print(f"{name}: Nj={circuit.junction_count()} status={status} iterations={info.get_number_of_iterations()}")
+
+
+def static_fixtures(pj):
+    # Newton iteration of static problems (StaticProblem.compute, static_problem.py:559-607):
+    # converging cases (s1-s3, s6) and two the reference's iteration gives up on (s4: bias above
+    # the critical current, no static state; s5: a poor initial guess)
+    a = pj.SquareArray(8, 7)
+    n = np.zeros(a.face_count(), int)
+    n[a.face_count() // 2] = 1
+    static_case(pj, "s1_square8x7_vortex", a, 0.3 * a.current_base(0.0), 0.05, n)
+    h = pj.HoneycombArray(4, 4)
+    h.set_inductance(0.3)
+    static_case(pj, "s2_honeycomb4x4_inductance", h, 0.0, 0.2, 0)
+    t = pj.TriangularArray(5, 5)
+    t.set_critical_current(np.random.default_rng(8).lognormal(0.0, 0.2, t.junction_count()))
+    static_case(pj, "s3_triangular5x5_disorder", t, 0.3 * t.current_base(np.pi / 2), 0.05, 0)
+    a = pj.SquareArray(6, 6)
+    static_case(pj, "s4_square6_overbias", a, 3.0 * a.current_base(0.0), 0.0, 0)
+    a = pj.SquareArray(7, 6)
+    a.set_inductance(np.random.default_rng(9).uniform(0.05, 0.4, a.junction_count()))
+    rng = np.random.default_rng(10)
+    guess = rng.uniform(-0.3, 0.3, a.junction_count())
+    static_case(pj, "s5_square7x6_guess", a, 0.2 * a.current_base(0.3), rng.uniform(0, 0.3, a.face_count()), 0,
+                initial_guess=guess, tol=1e-12, maxiter=40)
+    a = pj.SquareArray(12, 10)
+    a.set_inductance(0.2)
+    n = np.zeros(a.face_count(), int)
+    n[40] = 1
+    static_case(pj, "s6_square12x10_inductance_vortex", a, 0.2 * a.current_base(0.0), 0.05, n)
 
 
 def anneal_fixtures(pj):

@@ -10,7 +10,8 @@
     only to within that spread by any FP64 evaluation;
   - the IV-curve point V-bar = mean over horizontal junctions of (theta_9999 - theta_4999) /
     (dt 5000): within 1e-6 per problem;
-  - vortex configurations at step 9999 equal.
+  - vortex configurations at step 1999 equal (by step 9999 the running states have moved
+    apart chaotically; the time-averaged voltage does not feel it).
 * Large single array (SquareArray(1024, 1024), C = 0.5, L = 0.05, f = 0.1, bias 0.5 and 1.2 x
   current_base(0), T = 0): 24 steps, |dtheta| <= 1e-9 max(1, |theta|). This is the largest
   factor the library builds in any test (about 5e7 values, supernodes over 1500 columns wide).
@@ -53,8 +54,11 @@ def test_iv_sweep_full_length_against_oracle():
     horiz = np.arange(PJ.IV_N * (PJ.IV_N - 1))
     vbar = lambda th: (th[horiz, :, 2] - th[horiz, :, 1]).mean(0) / (PJ.IV_DT * (NT // 2))
     assert np.abs(vbar(th_g) - vbar(th_o)).max() <= 1e-6
+    # vortex configurations where the trajectories are defined to 1e-9 (after 2000 steps); by
+    # step 9999 the running states have moved apart chaotically (up to 1e-3 relative, the same
+    # for two orderings of the oracle), which the time average above does not feel
     A = p.get_circuit().get_cycle_matrix()
-    vort = lambda th: -(A @ np.round(th[:, :, 2] / (2 * np.pi)))
+    vort = lambda th: -(A @ np.round(th[:, :, 0] / (2 * np.pi)))
     assert np.array_equal(vort(th_g), vort(th_o))
 
 
