@@ -88,7 +88,8 @@ typedef struct {
   int min_piece;      /* shortest piece of a split dot product (default 16) */
   int schedule;       /* 1: one launch per elimination-tree level; 2: dataflow, one persistent
                          launch per sweep whose work items wait (bounded) on per-supernode
-                         completion counters; 0: default (1) */
+                         completion counters; 3: cooperative, one launch per sweep that walks the
+                         levels separated by bounded grid-wide barriers; 0: default (1) */
   int rows_per_lane_fwd; /* rows per lane of the forward sweep alone (0: rows_per_lane if set,
                             else the forward default: 2 for W >= 256, 1 below) */
   int pack_rows;      /* W = 1, level schedule: supernodes of at most this many rows (and at most 8
@@ -103,6 +104,8 @@ typedef struct {
                          on its own stream (created by the plan; the call's stream forks to them
                          and joins back before jja_run returns), so their launch chains overlap;
                          0: default (W / 160 clamped to [2, 4] from W = 256 on, else 1) */
+  int coop_blocks;    /* cooperative schedule: at most this many blocks per sweep launch (0: two per
+                         SM, fewer when the widest level has fewer work items) */
 } jja_solve_tuning;
 
 /* Builds on the host (no GPU needed) the work-item schedule that jja_plan_create would make for
@@ -146,9 +149,11 @@ int64_t jja_plan_device_bytes(const jja_plan* p);
  * in an input, or a time step too large for the circuit); the state is then invalid. */
 int jja_plan_check(jja_plan* p, int* flow_timeouts);
 /* Test of the bounded waits: runs one forward dataflow sweep whose wait counts can never be
- * reached, then synchronises `stream`. Every wait gives up (the first after its bound, the rest
- * at once), the kernel returns, and the plan's error flag is set for jja_plan_check to report.
- * The plan's face-space work vectors hold garbage afterwards; the plan stays usable. */
+ * reached (a plan of the cooperative schedule: one cooperative sweep whose grid barriers wait for
+ * one block more than the launch has), then synchronises `stream`. Every wait gives up (the
+ * first after its bound, the rest at once), the kernel returns, and the plan's error flag is set
+ * for jja_plan_check to report. The plan's face-space work vectors hold garbage afterwards; the
+ * plan stays usable. */
 int jja_plan_test_wait_limit(jja_plan* p, void* stream);
 
 /* A source on the device: at step i, value(n, w) = ptr[n*stride_n + w*stride_w + (i - t0)*stride_t]

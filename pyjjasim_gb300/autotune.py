@@ -3,8 +3,9 @@
 No counterpart in the reference (its solve is scipy's SuperLU). The cost of a time step on the
 GPU depends on choices that have no single best value across array sizes and batch widths W:
 
-* ``schedule``: one launch per elimination-tree level, or one persistent dataflow launch per
-  sweep whose work items wait on per-supernode completion counters (no gaps between levels);
+* ``schedule``: one launch per elimination-tree level, one persistent dataflow launch per
+  sweep whose work items wait on per-supernode completion counters, or one cooperative launch
+  per sweep with grid-wide barriers between the levels (no launch gaps between levels);
 * ``pdl``: programmatic dependent launch of the step's kernels (launch latency hidden behind
   the previous kernel's tail; pays off when the kernels are short);
 * ``ordering``: nested dissection (shallow tree, big supernodes) or minimum degree (about 30 %
@@ -63,7 +64,7 @@ def candidates(W):
     """Values tried per axis (the first is the default)."""
     wb = default_rhs_block(W)
     return {
-        "schedule": [1, 2],
+        "schedule": [1, 2, 3],
         "pdl": [0, 1],
         "ordering": ["auto", "nd", "mmd"],
         "groups": [0, 1, 2, 3, 4] if W >= 64 else [0],

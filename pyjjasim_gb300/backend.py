@@ -208,7 +208,7 @@ class GpuSimulation:
     ``run_timed`` advances with per-stage CUDA-event timing, ``theta`` returns the newest phase.
     """
 
-    def __init__(self, problem, noise="philox", seed=None, device=None, nd_leaf=8, stream=None, ordering="auto",
+    def __init__(self, problem, noise="philox", seed=None, device=None, nd_leaf=None, stream=None, ordering="auto",
                  relax=(-1, -1.0), Ic=None, tuning=None, tune=False):
         """``Ic``: optional (Nj, W) critical currents per problem, replacing the circuit's
         (problems then differ in Ic but share the face-space matrix, which does not depend on Ic).
@@ -390,7 +390,7 @@ class GpuSimulation:
 
 
 def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", seed=None, device=None,
-                        use_graph=True, nd_leaf=8, stream=None, ordering="auto", relax=(-1, -1.0), Ic=None,
+                        use_graph=True, nd_leaf=None, stream=None, ordering="auto", relax=(-1, -1.0), Ic=None,
                         tuning=None, tune=False, sim=None):
     """GPU time-stepping core; see the module docstring for the contract.
 

@@ -599,7 +599,7 @@ struct FactorDev {
 // reads 256 contiguous bytes while each lane walks its own supernode. Levels with many more
 // small supernodes than a wave of warps use them: a regular item there leaves most lanes idle and
 // pays a chain of dependent loads for a handful of FMAs. KM (>= KP) sizes the register arrays.
-template <int KM>
+template <int KM, bool kSharedLaunch>
 __device__ __forceinline__ void fwd_pack(const FactorDev& F, const int4 raw, int lane, double* __restrict__ b,
                                          double* __restrict__ z) {
   if (lane >= raw.y) return;
@@ -611,7 +611,7 @@ __device__ __forceinline__ void fwd_pack(const FactorDev& F, const int4 raw, int
   // of this level writes them
   double bv[KM];
 #pragma unroll
-  for (int j = 0; j < KM; ++j) bv[j] = j < k ? __ldg(b + c0 + j) : 0.0;
+  for (int j = 0; j < KM; ++j) bv[j] = j < k ? load_vec<kSharedLaunch>(b + c0 + j) : 0.0;
   const double* V = F.pack_vals + (int64_t)raw.w * 32 + lane;
   // rows unrolled so that about 16 loads of each lane are in flight
 #pragma unroll(16 / KM)
@@ -625,7 +625,7 @@ __device__ __forceinline__ void fwd_pack(const FactorDev& F, const int4 raw, int
   }
 }
 
-template <int KM>
+template <int KM, bool kSharedLaunch>
 __device__ __forceinline__ void bwd_pack(const FactorDev& F, const int4 raw, int lane, const double* __restrict__ z,
                                          double* __restrict__ x) {
   if (lane >= raw.y) return;
@@ -642,7 +642,7 @@ __device__ __forceinline__ void bwd_pack(const FactorDev& F, const int4 raw, int
   for (int r = 0; r < NP; ++r) {
     double v = 0.0;
     if (r < k) v = __ldg(z + c0 + r);
-    else if (r < nf) v = -__ldg(x + __ldg(R + (r - k)));
+    else if (r < nf) v = -load_vec<kSharedLaunch>(x + __ldg(R + (r - k)));
 #pragma unroll
     for (int i = 0; i < KM; ++i)
       if (i < KP) acc[i] = fma(__ldg(V + ((int64_t)i * NP + r) * 32), v, acc[i]);
@@ -652,20 +652,22 @@ __device__ __forceinline__ void bwd_pack(const FactorDev& F, const int4 raw, int
     if (i < k) x[c0 + i] = acc[i];
 }
 
+template <bool kSharedLaunch>
 __device__ __forceinline__ void fwd_pack_any(const FactorDev& F, const int4 raw, int lane, double* __restrict__ b,
                                              double* __restrict__ z) {
   const int KP = raw.z >> 16;
-  if (KP <= 2) fwd_pack<2>(F, raw, lane, b, z);
-  else if (KP <= 4) fwd_pack<4>(F, raw, lane, b, z);
-  else fwd_pack<kPackMaxK>(F, raw, lane, b, z);
+  if (KP <= 2) fwd_pack<2, kSharedLaunch>(F, raw, lane, b, z);
+  else if (KP <= 4) fwd_pack<4, kSharedLaunch>(F, raw, lane, b, z);
+  else fwd_pack<kPackMaxK, kSharedLaunch>(F, raw, lane, b, z);
 }
 
+template <bool kSharedLaunch>
 __device__ __forceinline__ void bwd_pack_any(const FactorDev& F, const int4 raw, int lane,
                                              const double* __restrict__ z, double* __restrict__ x) {
   const int KP = raw.z >> 16;
-  if (KP <= 2) bwd_pack<2>(F, raw, lane, z, x);
-  else if (KP <= 4) bwd_pack<4>(F, raw, lane, z, x);
-  else bwd_pack<kPackMaxK>(F, raw, lane, z, x);
+  if (KP <= 2) bwd_pack<2, kSharedLaunch>(F, raw, lane, z, x);
+  else if (KP <= 4) bwd_pack<4, kSharedLaunch>(F, raw, lane, z, x);
+  else bwd_pack<kPackMaxK, kSharedLaunch>(F, raw, lane, z, x);
 }
 
 // One forward work item (one warp): rows [r0, r1) of F_s b_s; diagonal rows go to z, the
@@ -812,7 +814,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_fwd_level(FactorDev F, 
   const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (it >= n_items) return;
   const int4 raw = items[it];
-  if (kPacks && raw.x < 0) fwd_pack_any(F, raw, threadIdx.x & 31, b, z);
+  if (kPacks && raw.x < 0) fwd_pack_any<false>(F, raw, threadIdx.x & 31, b, z);
   else fwd_item<kRowsPerLane, false>(F, unpack_item(raw), threadIdx.x & 31, W, WB, b, z);
 }
 
@@ -824,7 +826,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
   const int it = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (it >= n_items) return;
   const int4 raw = items[it];
-  if (kPacks && raw.x < 0) bwd_pack_any(F, raw, threadIdx.x & 31, z, x);
+  if (kPacks && raw.x < 0) bwd_pack_any<false>(F, raw, threadIdx.x & 31, z, x);
   else bwd_item<kRowsPerLane, false>(F, unpack_item(raw), threadIdx.x & 31, W, WB, z, x);
 }
 
@@ -898,6 +900,83 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_flow_sweep(FactorDev F,
       }
     }
     it = __shfl_sync(0xffffffffu, nxt, 0);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Cooperative sweeps (schedule 3): ONE launch per sweep that walks the elimination-tree levels
+// itself, separated by a grid-wide barrier instead of a kernel boundary. Few problems per launch
+// (a single array, a ragged union) leave the level kernels short and bound by their launch gaps
+// (~5 us per level replayed from a graph); a barrier costs about a microsecond. The launch is
+// cooperative, so all its blocks are resident at once and every block reaches every barrier.
+// Face vectors written by earlier levels of the same launch are read through L2 (ld.global.cg).
+// The barrier is a bounded spin: one that runs out sets the plan's error flag (jja_plan_check
+// reports it) and lets the launch finish; once one has run out, the others give up at once.
+// ------------------------------------------------------------------------------------------
+constexpr int kCoopThreads = 512;                    // 16 warps per block, at most 2 blocks per SM:
+constexpr int kCoopBlocksPerSM = 2;                  // few arrivals per barrier
+constexpr long long kBarrierSpinLimit = 1LL << 22;   // polls of >= 32 ns: >= 0.13 s, far beyond any level
+
+// the k-th barrier of a launch completes when the arrival counter (zero at the launch) reaches
+// (k + 1) x gridDim.x; `target` is that count
+__device__ __forceinline__ void grid_barrier(unsigned* count, unsigned target, int* err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();   // release: the block's writes (ordered by the CTA barrier) before the arrival
+    atomicAdd(count, 1u);
+    const volatile unsigned* c = count;
+    const volatile int* e = err;
+    for (long long i = 0; *c < target; ++i) {
+      if (i >= kBarrierSpinLimit || *e) {
+        atomicExch(err, 1);
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();   // acquire
+  }
+  __syncthreads();
+}
+
+// Phase 0 zeroes the rows that split dot products accumulate into (columns [w0, w0 + wn)) and
+// the other sweep's barrier counter (sweeps alternate forward, backward on a stream, so each
+// starts from a counter the previous one zeroed), then the levels run in order (forward: leaves
+// first; backward: root first), every warp of the grid taking the level's items in turn.
+template <int kRowsPerLane, bool kForward, bool kPacks>
+__global__ void __launch_bounds__(kCoopThreads) k_coop_sweep(FactorDev F, const int4* __restrict__ items,
+                                                             const int64_t* __restrict__ level_ptr, int n_levels,
+                                                             int W, int WB, double* b, double* z, double* x,
+                                                             const int32_t* __restrict__ zrows, int nz, int w0, int wn,
+                                                             unsigned* bar, unsigned* other_bar, int* err,
+                                                             unsigned unreachable) {
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+  double* acc = kForward ? z : x;
+  for (int64_t e = tid; e < (int64_t)nz * wn; e += nth) {
+    const int64_t i = e / wn, w = w0 + (e - i * wn);
+    acc[(int64_t)__ldg(zrows + i) * W + w] = 0.0;
+  }
+  if (tid == 0) *other_bar = 0u;
+  unsigned target = gridDim.x + unreachable;   // unreachable: 0, or 1 to test the barrier's bound
+  grid_barrier(bar, target, err);
+  const int64_t warp = tid >> 5, nwarps = nth >> 5;
+  const int lane = threadIdx.x & 31;
+  for (int q = 0; q < n_levels; ++q) {
+    const int l = kForward ? q : n_levels - 1 - q;
+    const int64_t i1 = __ldg(level_ptr + l + 1);
+    for (int64_t it = __ldg(level_ptr + l) + warp; it < i1; it += nwarps) {
+      const int4 raw = items[it];
+      if (kForward) {
+        if (kPacks && raw.x < 0) fwd_pack_any<true>(F, raw, lane, b, z);
+        else fwd_item<kRowsPerLane, true>(F, unpack_item(raw), lane, W, WB, b, z);
+      } else {
+        if (kPacks && raw.x < 0) bwd_pack_any<true>(F, raw, lane, z, x);
+        else bwd_item<kRowsPerLane, true>(F, unpack_item(raw), lane, W, WB, z, x);
+      }
+    }
+    if (q + 1 < n_levels) {
+      target += gridDim.x;
+      grid_barrier(bar, target, err);
+    }
   }
 }
 
@@ -1093,7 +1172,8 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
     if (v && v != 1 && v != 2 && v != 4 && v != 8)
       throw Error(JJA_ERR_ARG, "rows_per_lane and rows_per_lane_fwd must be 1, 2, 4 or 8");
   if (tu.target_warps < 0 || tu.min_piece < 0) throw Error(JJA_ERR_ARG, "target_warps and min_piece must be >= 0");
-  if (tu.schedule < 0 || tu.schedule > 2) throw Error(JJA_ERR_ARG, "schedule must be 0, 1 or 2");
+  if (tu.schedule < 0 || tu.schedule > 3) throw Error(JJA_ERR_ARG, "schedule must be 0, 1, 2 or 3");
+  if (tu.coop_blocks < 0) throw Error(JJA_ERR_ARG, "coop_blocks must be >= 0");
   if (tu.pdl < 0 || tu.pdl > 1) throw Error(JJA_ERR_ARG, "pdl must be 0 or 1");
   if (tu.pack_rows > 256) throw Error(JJA_ERR_ARG, "pack_rows must be <= 256");
   if (tu.pack_min_warps < 0) throw Error(JJA_ERR_ARG, "pack_min_warps must be >= 0");
@@ -1401,6 +1481,14 @@ struct jja_plan {
   unsigned* counters = nullptr;   // forward: [next, done[ns]], then backward: [next, done[ns]]
   int* flow_err = nullptr;
   int flow_blocks[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};   // resident blocks per (rows/lane 2,4,8,1) x (bwd, fwd)
+  // cooperative sweeps (schedule 3): level boundaries of `all` on the device, blocks per launch
+  // ([backward, forward][without, with W = 1 packs]), barrier arrival counters [backward, forward]
+  int coop = 0;
+  int64_t* coop_fwd_lp = nullptr;
+  int64_t* coop_bwd_lp = nullptr;
+  int coop_grid[2][2] = {{0, 0}, {0, 0}};
+  unsigned* coop_bar = nullptr;
+  bool coop_packs = false;
   int64_t bytes = 0;
   // captured graphs of a fixed-length step sequence, keyed by the buffers they bake in (a few
   // are kept: double-buffered source windows alternate between two keys), most recent last
@@ -1453,9 +1541,24 @@ void launch(bool pdl, void (*kernel)(KArgs...), int grid, int block, cudaStream_
   g_launches++;
 }
 
+// the cooperative sweep kernel of a rows-per-lane variant (for occupancy queries)
+const void* coop_kernel(int rpl, bool forward, bool packs) {
+#define JJA_COOP_K(R) \
+  (forward ? (packs ? (const void*)k_coop_sweep<R, true, true> : (const void*)k_coop_sweep<R, true, false>) \
+           : (packs ? (const void*)k_coop_sweep<R, false, true> : (const void*)k_coop_sweep<R, false, false>))
+  switch (rpl) {
+    case 1: return JJA_COOP_K(1);
+    case 2: return JJA_COOP_K(2);
+    case 8: return JJA_COOP_K(8);
+    default: return JJA_COOP_K(4);
+  }
+#undef JJA_COOP_K
+}
+
 // zero the rows that partial items of the coming sweep accumulate into (and, for a dataflow
 // sweep, its counters)
 void launch_zero_rows(jja_plan* p, const Group& g, cudaStream_t st, bool forward, double* v) {
+  if (p->coop) return;   // a cooperative sweep zeroes its rows in its first phase
   const int n = forward ? g.nz_f : g.nz_b;
   const int n_ctr = p->flow ? p->ns + 1 : 0;
   if (!n && !n_ctr) return;
@@ -1490,10 +1593,42 @@ void launch_flow(jja_plan* p, cudaStream_t st, bool forward, double* b, double* 
            p->W, p->WB, b, z, x, fl);
 }
 
+// a sweep as one cooperative launch over all levels (schedule 3; the group of all problems)
+template <int RPL>
+void launch_coop(jja_plan* p, cudaStream_t st, bool forward, double* b, double* z, double* x,
+                 unsigned unreachable = 0) {
+  const Group& g = p->all;
+  const bool packs = p->coop_packs;
+  void (*kern)(FactorDev, const int4*, const int64_t*, int, int, int, double*, double*, double*, const int32_t*, int,
+               int, int, unsigned*, unsigned*, int*, unsigned);
+  if (forward) kern = packs ? k_coop_sweep<RPL, true, true> : k_coop_sweep<RPL, true, false>;
+  else kern = packs ? k_coop_sweep<RPL, false, true> : k_coop_sweep<RPL, false, false>;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)p->coop_grid[forward][packs]);
+  cfg.blockDim = dim3((unsigned)kCoopThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  JJA_CUDA(cudaLaunchKernelEx(&cfg, kern, p->F, (const int4*)(forward ? g.fwd_items : g.bwd_items),
+                              (const int64_t*)(forward ? p->coop_fwd_lp : p->coop_bwd_lp), p->n_levels, p->W, p->WB, b,
+                              z, x, (const int32_t*)(forward ? g.zrows_f : g.zrows_b), forward ? g.nz_f : g.nz_b, g.w0,
+                              g.wn, p->coop_bar + (forward ? 1 : 0), p->coop_bar + (forward ? 0 : 1), p->flow_err,
+                              unreachable));
+  g_launches++;
+}
+
 template <int RPL>
 void launch_sweep(jja_plan* p, const Group& g, cudaStream_t st, bool forward, double* b, double* z, double* x) {
   if (p->flow) {
     launch_flow<RPL>(p, st, forward, b, z, x);
+    return;
+  }
+  if (p->coop) {
+    launch_coop<RPL>(p, st, forward, b, z, x);
     return;
   }
   if (forward) {  // levels ascending (children before parents); b is consumed, z produced
@@ -1880,7 +2015,7 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
       // 1.23 ms with 2 / 3 / 4; W = 1024 2.61 -> 2.36 / 2.31 ms with 2 / 4; W = 64 (64x64) no gain
       const int chunks = (d->W + p->WB - 1) / p->WB;
       int ng = tu.groups ? tu.groups : (d->W >= kGroupsFromW ? std::max(2, std::min(4, d->W / kGroupW)) : 1);
-      if (tu.schedule == 2) ng = 1;
+      if (tu.schedule == 2 || tu.schedule == 3) ng = 1;
       ng = std::max(1, std::min(ng, chunks));
       if (ng > 1) {
         p->groups.resize(ng);
@@ -1923,6 +2058,32 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
           p->flow_blocks[v][d] = std::max(1, occ) * nsm;
         }
       p->flow = (tu.schedule == 2) ? 1 : 0;
+      // cooperative sweeps: blocks per launch within what can be resident at once (2 per SM at
+      // most, fewer when the widest level has fewer items than the grid's warps, or as tuned)
+      p->coop = (tu.schedule == 3) ? 1 : 0;
+      if (p->coop) {
+        p->coop_fwd_lp = p->up(S.fwd_ptr.data(), S.fwd_ptr.size());
+        p->coop_bwd_lp = p->up(S.bwd_ptr.data(), S.bwd_ptr.size());
+        p->coop_bar = p->up<unsigned>(nullptr, 2);
+        JJA_CUDA(cudaMemset(p->coop_bar, 0, 2 * sizeof(unsigned)));
+        for (char c : S.level_packed) p->coop_packs |= c != 0;
+        int64_t widest[2] = {1, 1};
+        for (int l = 0; l < S.n_levels; ++l) {
+          widest[1] = std::max<int64_t>(widest[1], S.fwd_ptr[l + 1] - S.fwd_ptr[l]);
+          widest[0] = std::max<int64_t>(widest[0], S.bwd_ptr[l + 1] - S.bwd_ptr[l]);
+        }
+        for (int fw = 0; fw < 2; ++fw)
+          for (int pk = 0; pk < 2; ++pk) {
+            const void* k = coop_kernel(fw ? p->rows_per_lane_fwd : p->rows_per_lane, fw != 0, pk != 0);
+            int occ = 0;
+            JJA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kCoopThreads, 0));
+            if (occ < 1) throw Error(JJA_ERR_CUDA, "cooperative sweep kernel cannot be resident");
+            int64_t grid = (int64_t)std::min(occ, kCoopBlocksPerSM) * nsm;
+            grid = std::min<int64_t>(grid, (widest[fw] + kCoopThreads / 32 - 1) / (kCoopThreads / 32));
+            if (tu.coop_blocks) grid = std::min<int64_t>(grid, tu.coop_blocks);
+            p->coop_grid[fw][pk] = (int)std::max<int64_t>(1, grid);
+          }
+      }
     }
     const size_t NfW = (size_t)Nf * d->W, NjW = (size_t)Nj * d->W;
     p->b = p->up<double>(nullptr, NfW);
@@ -1943,6 +2104,15 @@ int jja_plan_test_wait_limit(jja_plan* p, void* stream) {
   return guarded([&] {
     if (!p) throw Error(JJA_ERR_ARG, "jja_plan_test_wait_limit: null plan");
     cudaStream_t st = (cudaStream_t)stream;
+    if (p->coop) {
+      // cooperative plan: a forward sweep whose barriers wait for one block more than the grid
+      // has; each gives up after its bound, and the counters are reset by the next sweeps
+      launch_coop<kDefaultRowsPerLane>(p, st, true, p->b, p->z, p->x, 1u);
+      JJA_CUDA(cudaStreamSynchronize(st));
+      JJA_CUDA(cudaMemsetAsync(p->coop_bar, 0, 2 * sizeof(unsigned), st));
+      JJA_CUDA(cudaStreamSynchronize(st));
+      return;
+    }
     const std::vector<uint32_t> never((size_t)std::max(p->ns, 1), 0xffffffffu);
     uint32_t* d = nullptr;
     JJA_CUDA(cudaMalloc(&d, never.size() * sizeof(uint32_t)));

@@ -29,8 +29,8 @@ _CACHE_LOCK = threading.Lock()   # the caches are shared by host threads (ragged
 EXTRAP = {3: (2.0, -1.0), 4: (3.0, -3.0, 1.0), 5: (4.0, -6.0, 4.0, -1.0)}
 # launch-shape fields of the triangular solves (jja_solve_tuning)
 TUNING_FIELDS = ("rhs_block", "rows_per_lane", "target_warps", "min_piece", "schedule", "rows_per_lane_fwd",
-                 "pack_rows", "pack_min_warps", "pdl", "groups")
-SCHEDULES = {"levels": 1, "dataflow": 2}
+                 "pack_rows", "pack_min_warps", "pdl", "groups", "coop_blocks")
+SCHEDULES = {"levels": 1, "dataflow": 2, "cooperative": 3}
 
 
 def _digest(*arrays):
@@ -173,7 +173,8 @@ class DevicePlan:
         t = ctypes.c_int(0)
         N.check(N.lib().jja_plan_check(self.handle, ctypes.byref(t)))
         if t.value:
-            raise N.JJAError(5, "a dataflow sweep's dependency wait ran out of its bound; results are invalid")
+            raise N.JJAError(5, "a bounded wait of a dataflow or cooperative sweep ran out of its bound; "
+                                "results are invalid")
 
     def eval_sin(self, x_dev, out_dev, n, stream=0):
         N.check(N.lib().jja_eval_sin(self.handle, ctypes.c_void_p(x_dev), ctypes.c_void_p(out_dev), int(n),
@@ -209,6 +210,25 @@ def resolve_ordering(ordering, W, n_faces):
     return ordering
 
 
+SMALL_STEP_FACES = 1 << 15   # W x Nf up to which "auto" factors with large leaves and strong amalgamation
+
+
+def resolve_factor_shape(nd_leaf, relax, ordering, W, n_faces):
+    """(nd_leaf, relax) that ``nd_leaf=None`` stands for. A step of few face-problems
+    (W x Nf <= 2^15, nested dissection, default amalgamation) is bound by the elimination tree's
+    depth: every level of each sweep is a chain of dependent memory round trips (about 3.5 us on
+    GB300), and the flops are negligible. Such steps factor with nested-dissection leaves of 128
+    faces and merge supernodes that add at most 256 zeros or 50 %: fewer, denser levels. Measured
+    (W = 1, graph-replayed steps): SquareArray(10,10) 0.029 -> 0.014 ms/step (one dense
+    supernode), SquareArray(128,128) 0.113 -> 0.081 ms; at 256x256 the larger factor costs more
+    than the levels it saves (0.165 -> 0.205 ms), so larger steps keep leaves of 8."""
+    if nd_leaf is not None:
+        return nd_leaf, relax
+    if ordering == "nd" and tuple(relax) == (-1, -1.0) and W * n_faces <= SMALL_STEP_FACES:
+        return 128, (256, 0.5)
+    return 8, relax
+
+
 def fill_reducing_order(K, ordering, circuit=None):
     """(coords, perm) for HostFactor. "nd": the library's nested dissection on face centroids;
     "mmd": the multiple-minimum-degree column order scipy's SuperLU computes on A + A^T
@@ -240,12 +260,14 @@ def get_factor(circuit, dt, nd_leaf=8, ordering="nd", relax=(-1, -1.0)):
     return f, A, key
 
 
-def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=8, ordering="auto", relax=(-1, -1.0), Ic_w=None,
+def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=None, ordering="auto", relax=(-1, -1.0), Ic_w=None,
              tuning=None):
     """Device plan for W problems; ``Ic_w`` (Nj, W) gives each problem its own critical currents;
-    ``ordering`` "nd", "mmd" or "auto" (see resolve_ordering); ``tuning`` the launch shape of the
-    triangular solves (see DevicePlan)."""
+    ``ordering`` "nd", "mmd" or "auto" (see resolve_ordering); ``nd_leaf`` None: by the step's
+    size (see resolve_factor_shape); ``tuning`` the launch shape of the triangular solves (see
+    DevicePlan)."""
     ordering = resolve_ordering(ordering, W, circuit._Nf())
+    nd_leaf, relax = resolve_factor_shape(nd_leaf, relax, ordering, W, circuit._Nf())
     factor, A, fkey = get_factor(circuit, dt, nd_leaf, ordering=ordering, relax=relax)
     Rv, Cv, coef = coefficients(circuit, dt, stencil)
     if Ic_w is not None:
