@@ -305,6 +305,50 @@ def large_array_leg(G, torch, steps, base, oracle_job=None):
     return out
 
 
+def static_leg(G, torch, n=64, W=64, oracle_sample=6):
+    """The static (Newton) solver: W static problems on one SquareArray(n, n), L = 0.1, bias
+    current_base(angle) x 0.05-0.3 at angles spread over [0, pi), f = 0, 0.01 or 0.02, no target
+    vortex (the reference's iteration solves about two thirds of them from its London guess, in
+    1-8 iterations, and gives up on the rest), solved together by
+    the batched device iteration (StaticProblem.compute per problem in the reference). Timed end
+    to end (London guesses, every Newton iteration's refactorisation and solve, residuals) after a
+    warm-up batch; the oracle (scipy SuperLU per iteration, as the reference) times
+    `oracle_sample` of the problems and checks their status and phases."""
+    from oracle import static_oracle as SO
+    from pyjjasim_gb300.static import StaticProblem, compute_many
+    a = G.SquareArray(n, n)
+    a.set_inductance(0.1)
+    spec = [(0.05 + 0.25 * (w % 6) / 5, np.pi * w / W, 0.01 * (w % 3)) for w in range(W)]
+    probs = [StaticProblem(a, current_sources=b * a.current_base(ang), external_flux=f) for b, ang, f in spec]
+    compute_many(probs[:W])                       # plan, symbolic factor, module load
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = compute_many(probs)
+    t_gpu = time.perf_counter() - t0
+    iters = [info.get_number_of_iterations() for _, _, info in out]
+    status = [st for _, st, _ in out]
+    A, M = a.get_cycle_matrix(), a.get_cut_matrix()
+    t0 = time.perf_counter()
+    agree = True
+    for w in range(oracle_sample):
+        p = probs[w]
+        g = p.approximate().get_theta()
+        th, st, res, _ = SO.static_compute(A, M, a._L(), a._Ic(), g, p._Is(), p._f(), p._nt())
+        d = (th - out[w][0].get_theta()) / (2 * np.pi)
+        agree &= st == status[w] and (st != 0 or float(np.abs(d - np.round(d)).max()) < 1e-9)
+    t_cpu = (time.perf_counter() - t0) / oracle_sample
+    return {"workload": f"{W} static problems on SquareArray({n},{n}), L=0.1, bias 0.05-0.3 x current_base(angle), "
+                        f"f 0, 0.01 or 0.02, target n = 0; Newton iteration of the reference (tol 1e-10, maxiter 30)",
+            "problems": W, "Nj": a._Nj(), "gpu_seconds": t_gpu, "problems_per_s": W / t_gpu,
+            "newton_iterations": {"min": int(min(iters)), "max": int(max(iters)), "mean": float(np.mean(iters))},
+            "converged": int(sum(1 for st in status if st == 0)),
+            "oracle_seconds_per_problem": t_cpu, "oracle_problems_per_s": 1.0 / t_cpu,
+            "gpu_over_oracle": (W / t_gpu) * t_cpu,
+            "oracle_sample_agrees": bool(agree),
+            "oracle": "numpy/scipy restatement of static_compute (pinned to the reference's StaticProblem fixtures), "
+                      "one problem at a time on one core"}
+
+
 def ragged_draws():
     """The ragged batch's seeded draws: lattice kind (square / honeycomb / triangular) and side."""
     rng = np.random.default_rng(7)
@@ -607,6 +651,8 @@ def main():
     ap.add_argument("--ragged-problems", type=int, default=256,
                     help="problems of the ragged leg, the first of 256 seeded draws (0 skips it)")
     ap.add_argument("--ragged-steps", type=int, default=200, help="timed steps of the ragged leg")
+    ap.add_argument("--static-problems", type=int, default=64,
+                    help="problems of the static (Newton) solver leg (0 skips it)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -790,6 +836,8 @@ def main():
         if args.large_steps > 0:
             legs.append(("single_1024x1024_w8", lambda: large_array_leg(
                 G, torch, args.large_steps, jobs["large_base"].get(), jobs.get("large"))))
+        if args.static_problems > 0:
+            legs.append(("static_newton_64x64", lambda: static_leg(G, torch, W=args.static_problems)))
         if args.ragged_problems > 0:
             legs.append(("ragged", lambda: ragged_leg(
                 G, torch, args.ragged_problems, args.ragged_steps,

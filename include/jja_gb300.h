@@ -142,6 +142,14 @@ int jja_plan_create(const jja_plan_desc* desc, const jja_factor* f, jja_plan** o
 void jja_plan_destroy(jja_plan* p);
 /* Bytes of device memory held by the plan (tables + factor + work vectors). */
 int64_t jja_plan_device_bytes(const jja_plan* p);
+/* Fast Poisson solve of uniform square arrays (the row SquareArray reserves for it,
+ * josephson_circuit.py:958 `_Asq_dst_K`): when K = kappa (4 I - adjacency) on an mx x my grid of
+ * faces (equal R and C, a uniform self-inductance; K = kappa times the 5-point Dirichlet
+ * Laplacian), every face-space solve of the plan (time steps, jja_solve, the adjoint) becomes
+ * three sine-transform kernels instead of the triangular sweeps. grid_face[iy * mx + ix] (host,
+ * mx * my entries): the face (original order) at grid cell (ix, iy); mx + 1 and my + 1 powers of
+ * two up to 1024. The caller checks that K has that form. jja_solve_static keeps the sweeps. */
+int jja_plan_set_fast_poisson(jja_plan* p, int mx, int my, const int32_t* grid_face, double kappa);
 /* Synchronises the device, then reads and clears the plan's device error flags: *flow_timeouts
  * = 1 if a wait of a dataflow sweep ran out of its bound since the last call (the results of
  * those steps are invalid), else 0. Returns JJA_ERR_NONFINITE when a time step of jja_run /

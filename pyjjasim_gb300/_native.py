@@ -96,6 +96,7 @@ SIGNATURES = {
     "jja_plan_create": (c_int, [ctypes.POINTER(PlanDesc), c_void_p, ctypes.POINTER(c_void_p)]),
     "jja_plan_destroy": (None, [c_void_p]),
     "jja_plan_device_bytes": (c_int64, [c_void_p]),
+    "jja_plan_set_fast_poisson": (c_int, [c_void_p, c_int, c_int, P_i32, c_double]),
     "jja_plan_check": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
     "jja_plan_test_wait_limit": (c_int, [c_void_p, c_void_p]),
     "jja_run": (c_int, [c_void_p, ctypes.POINTER(State), c_int, P_i64, P_i64, c_int, c_void_p]),

@@ -209,12 +209,13 @@ class GpuSimulation:
     """
 
     def __init__(self, problem, noise="philox", seed=None, device=None, nd_leaf=None, stream=None, ordering="auto",
-                 relax=(-1, -1.0), Ic=None, tuning=None, tune=False):
+                 relax=(-1, -1.0), Ic=None, tuning=None, tune=False, fast_poisson="auto"):
         """``Ic``: optional (Nj, W) critical currents per problem, replacing the circuit's
         (problems then differ in Ic but share the face-space matrix, which does not depend on Ic).
         ``tuning``: launch shape of the triangular solves (plan.TUNING_FIELDS); ``tune=True``
         takes ``relax`` and ``tuning`` from the autotuner (timed once per GPU, circuit and W,
-        then cached on disk)."""
+        then cached on disk). ``fast_poisson``: sine-transform face solves for uniform square
+        arrays (plan.get_plan): "auto", True or False."""
         stage = self.stage = HostStage(problem)       # host reads first: no CUDA call before
         torch = self.torch = _torch()
         c = stage.circuit
@@ -232,7 +233,8 @@ class GpuSimulation:
             self.relax, self.tuning = tuple(relax), dict(tuning or {})
             self.stream = stream if stream is not None else torch.cuda.Stream(device=self.dev)
             self.plan = P.get_plan(c, stage.dt, self.W, self.width, stage.stencil, nd_leaf=nd_leaf,
-                                   ordering=self.ordering, relax=relax, Ic_w=Ic, tuning=tuning)
+                                   ordering=self.ordering, relax=relax, Ic_w=Ic, tuning=tuning,
+                                   fast_poisson=fast_poisson)
             self.hist0, self.hist0_zero = stage.hist0, stage.hist0_zero
             self.hist = []
             with torch.cuda.stream(self.stream):
@@ -391,7 +393,7 @@ class GpuSimulation:
 
 def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", seed=None, device=None,
                         use_graph=True, nd_leaf=None, stream=None, ordering="auto", relax=(-1, -1.0), Ic=None,
-                        tuning=None, tune=False, sim=None):
+                        tuning=None, tune=False, sim=None, fast_poisson="auto"):
     """GPU time-stepping core; see the module docstring for the contract.
 
     ``ordering`` ("nd", "mmd" or "auto": minimum degree when W x Nf >= 2^22 on up to 2^18 faces,
@@ -401,7 +403,7 @@ def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", se
     GpuSimulation of this problem, already built (its own options apply)."""
     if sim is None:
         sim = GpuSimulation(problem, noise=noise, seed=seed, device=device, nd_leaf=nd_leaf, stream=stream,
-                            ordering=ordering, relax=relax, Ic=Ic, tuning=tuning, tune=tune)
+                            ordering=ordering, relax=relax, Ic=Ic, tuning=tuning, tune=tune, fast_poisson=fast_poisson)
     elif sim.problem is not problem:
         raise ValueError("time_evolution_core: the simulation belongs to another problem")
     torch = sim.torch
@@ -457,9 +459,9 @@ def time_evolution_core(problem, th_store_mask, I_store_mask, noise="philox", se
     return th_buf.transpose(1, 2, 0), I_buf.transpose(1, 2, 0)
 
 
-def solve_faces(circuit, dt, b, stencil_width=3, nd_leaf=8, ordering="auto", tuning=None):
+def solve_faces(circuit, dt, b, stencil_width=3, nd_leaf=8, ordering="auto", tuning=None, fast_poisson=False):
     """K^{-1} b on the GPU for (Nf, W) right-hand sides (the per-step face-space solve);
-    ``ordering`` and ``tuning`` as for the simulation's plan."""
+    ``ordering``, ``tuning`` and ``fast_poisson`` as for the simulation's plan."""
     from .problem import stencil
     torch = _torch()
     b = np.ascontiguousarray(b, np.float64)
@@ -468,7 +470,7 @@ def solve_faces(circuit, dt, b, stencil_width=3, nd_leaf=8, ordering="auto", tun
         b = b[:, None]
     W = b.shape[1]
     pl = P.get_plan(circuit, dt, W, stencil_width, stencil(stencil_width), nd_leaf=nd_leaf, ordering=ordering,
-                    tuning=tuning)
+                    tuning=tuning, fast_poisson=fast_poisson)
     st = torch.cuda.Stream()
     with torch.cuda.stream(st):
         bd = torch.from_numpy(b).cuda()

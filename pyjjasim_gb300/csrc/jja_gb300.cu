@@ -981,6 +981,102 @@ __global__ void __launch_bounds__(kCoopThreads) k_coop_sweep(FactorDev F, const 
 }
 
 // ------------------------------------------------------------------------------------------
+// Fast Poisson solve for uniform square arrays. With equal R, C and a uniform self-inductance l,
+// K = kappa (4 I - adjacency) on the (mx x my) grid of faces, kappa = l + 1/(Cv + Rv): the
+// 5-point Laplacian with Dirichlet boundaries, diagonalised by the sine transform (DST-I) along
+// rows and columns, eigenvalues kappa (lx_kx + ly_ky), l_k = 2 - 2 cos(pi k / (m + 1)). A solve
+// is three kernels and reads no factor: DST of every face row; per column DST, division by the
+// eigenvalues (and the transforms' scale), inverse DST; inverse DST of every row. Each DST-I of
+// length m = N - 1 is the imaginary part of a radix-2 FFT of the odd extension (length 2N, N a
+// power of two) in shared memory: y_k = -Im(FFT(e))_k / 2, e = (0, x, 0, -reverse(x)).
+// (A sparse supernodal solve of the same matrix is a chain of tree levels, each a few dependent
+// memory round trips; three short launches beat it for few problems per launch.)
+// ------------------------------------------------------------------------------------------
+struct DstArgs {
+  int mx, my;                  // faces per grid row, grid rows
+  int lgx, lgy;                // log2 of the FFT lengths 2 (mx + 1), 2 (my + 1)
+  const int32_t* grid_face;    // per cell iy * mx + ix: the face (factor's order)
+  const double2* twx;          // exp(-2 pi i k / (2 (mx + 1))), k < mx + 1
+  const double2* twy;
+  const double* lamx;          // 2 - 2 cos(pi (k + 1) / (mx + 1)), k < mx
+  const double* lamy;
+  double scale;                // (2 / (mx + 1)) (2 / (my + 1)) / kappa
+  double* t1;                  // scratch, (W, my, mx) problem-major
+  double* t2;
+};
+
+// load the odd extension of x (m values at x[j * stride]) into a (bit-reversed order), then
+// transform; on return -Im(a[k]) / 2, k = 1..m, is the DST-I of x
+__device__ __forceinline__ void dst_line(double2* a, const double* x, int64_t stride, int m, int lg,
+                                         const double2* __restrict__ tw) {
+  const int n = 2 * (m + 1), N = m + 1;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double e = 0.0;
+    if (i >= 1 && i <= m) e = x[(int64_t)(i - 1) * stride];
+    else if (i > N) e = -x[(int64_t)(n - i - 1) * stride];
+    a[__brev((unsigned)i) >> (32 - lg)] = make_double2(e, 0.0);
+  }
+  __syncthreads();
+  for (int l = 1; l <= lg; ++l) {
+    const int half = 1 << (l - 1), tstride = n >> l;
+    for (int j = threadIdx.x; j < n / 2; j += blockDim.x) {
+      const int pos = j & (half - 1);
+      const int i0 = ((j >> (l - 1)) << l) + pos, i1 = i0 + half;
+      const double2 w = __ldg(tw + pos * tstride);
+      const double2 u = a[i0], v = a[i1];
+      const double2 t = make_double2(fma(w.x, v.x, -w.y * v.y), fma(w.x, v.y, w.y * v.x));
+      a[i0] = make_double2(u.x + t.x, u.y + t.y);
+      a[i1] = make_double2(u.x - t.x, u.y - t.y);
+    }
+    __syncthreads();
+  }
+}
+
+// rows: out(w, iy, k) = DST_x of row iy of problem w0 + blockIdx.y; `in_faces`: the input is a
+// face vector (N x W, factor's face order) read through grid_face, else a (W, my, mx) scratch;
+// `out_faces` likewise for the output
+__global__ void k_dst_rows(DstArgs d, const double* in, double* out, int W, int w0, int in_faces, int out_faces) {
+  extern __shared__ double2 fft_buf[];
+  const int iy = blockIdx.x, w = w0 + blockIdx.y;
+  const double* src;
+  int64_t stride;
+  if (in_faces) {
+    // gather the row through the face map into the tail of the buffer's real parts first
+    double* row = reinterpret_cast<double*>(fft_buf + 2 * (d.mx + 1));
+    for (int j = threadIdx.x; j < d.mx; j += blockDim.x) row[j] = in[(int64_t)__ldg(d.grid_face + iy * d.mx + j) * W + w];
+    __syncthreads();
+    src = row;
+    stride = 1;
+  } else {
+    src = in + ((int64_t)w * d.my + iy) * d.mx;
+    stride = 1;
+  }
+  dst_line(fft_buf, src, stride, d.mx, d.lgx, d.twx);
+  for (int k = threadIdx.x; k < d.mx; k += blockDim.x) {
+    const double y = -0.5 * fft_buf[k + 1].y;
+    if (out_faces) out[(int64_t)__ldg(d.grid_face + iy * d.mx + k) * W + w] = y;
+    else out[((int64_t)w * d.my + iy) * d.mx + k] = y;
+  }
+}
+
+// columns: DST_y, division by the eigenvalues times the scale, inverse DST_y (DST-I is its own
+// inverse up to the scale)
+__global__ void k_dst_cols(DstArgs d, int w0) {
+  extern __shared__ double2 fft_buf[];
+  const int kx = blockIdx.x, w = w0 + blockIdx.y;
+  const double* col = d.t1 + (int64_t)w * d.my * d.mx + kx;
+  double* tmp = reinterpret_cast<double*>(fft_buf + 2 * (d.my + 1));   // my values after the FFT buffer
+  dst_line(fft_buf, col, d.mx, d.my, d.lgy, d.twy);
+  const double lx = __ldg(d.lamx + kx);
+  for (int k = threadIdx.x; k < d.my; k += blockDim.x)
+    tmp[k] = -0.5 * fft_buf[k + 1].y * d.scale / (lx + __ldg(d.lamy + k));
+  __syncthreads();
+  dst_line(fft_buf, tmp, 1, d.my, d.lgy, d.twy);
+  double* out = d.t2 + (int64_t)w * d.my * d.mx + kx;
+  for (int k = threadIdx.x; k < d.my; k += blockDim.x) out[(int64_t)k * d.mx] = -0.5 * fft_buf[k + 1].y;
+}
+
+// ------------------------------------------------------------------------------------------
 // Adjoint (backward through time) of the width-3 step theta_n = Q x_n + const, with
 // x_n = Ic sin(phi_n) + c1 th_{n-1} + c2 th_{n-2} - Is, phi_n = 2 th_{n-1} - th_{n-2},
 // Q = D A^T K^-1 A D - D, D = diag(1/c0) (symmetric, so Q^T = Q and one factor serves).
@@ -1489,6 +1585,10 @@ struct jja_plan {
   int coop_grid[2][2] = {{0, 0}, {0, 0}};
   unsigned* coop_bar = nullptr;
   bool coop_packs = false;
+  // fast Poisson solve of uniform square arrays (jja_plan_set_fast_poisson): replaces both sweeps
+  int dst = 0;
+  DstArgs dst_args{};
+  std::vector<int32_t> iperm_host;   // original face -> factor's face order
   int64_t bytes = 0;
   // captured graphs of a fixed-length step sequence, keyed by the buffers they bake in (a few
   // are kept: double-buffered source windows alternate between two keys), most recent last
@@ -1671,6 +1771,25 @@ void launch_levels(jja_plan* p, const Group& g, cudaStream_t st, bool forward) {
 
 void launch_levels(jja_plan* p, cudaStream_t st, bool forward) { launch_levels(p, p->all, st, forward); }
 
+// x = K^-1 b for group g: the two triangular sweeps, or the three sine-transform kernels
+void launch_face_solve(jja_plan* p, const Group& g, cudaStream_t st) {
+  if (!p->dst) {
+    launch_levels(p, g, st, true);
+    launch_levels(p, g, st, false);
+    return;
+  }
+  const DstArgs& d = p->dst_args;
+  const size_t smx = (size_t)2 * (d.mx + 1) * sizeof(double2) + (size_t)d.mx * sizeof(double);
+  const size_t smy = (size_t)2 * (d.my + 1) * sizeof(double2) + (size_t)d.my * sizeof(double);
+  const int tx = std::min(512, d.mx + 1), ty = std::min(512, d.my + 1);
+  k_dst_rows<<<dim3((unsigned)d.my, (unsigned)g.wn), tx, smx, st>>>(d, p->b, d.t1, p->W, g.w0, 1, 0);
+  k_dst_cols<<<dim3((unsigned)d.mx, (unsigned)g.wn), ty, smy, st>>>(d, g.w0);
+  k_dst_rows<<<dim3((unsigned)d.my, (unsigned)g.wn), tx, smx, st>>>(d, d.t2, p->x, p->W, g.w0, 0, 1);
+  g_launches += 3;
+}
+
+void launch_face_solve(jja_plan* p, cudaStream_t st) { launch_face_solve(p, p->all, st); }
+
 // q of the first step of a run, from the phase history (the args' group of problems)
 void launch_junction(jja_plan* p, StepArgs& a, cudaStream_t st) {
   launch(p->pdl, k_junction, grid_for((int64_t)p->Nj * a.wn, 256), 256, st, a, p->t, p->xj);
@@ -1685,9 +1804,14 @@ void launch_step(jja_plan* p, const Group& g, StepArgs& a, cudaStream_t st, bool
   if (ev) JJA_CUDA(cudaEventRecord(ev[0], st));
   launch(p->pdl, k_face_rhs, grid_for(nf, 256), 256, st, a, p->t, (const double*)p->xj, p->b);
   if (ev) JJA_CUDA(cudaEventRecord(ev[1], st));
-  launch_levels(p, g, st, true);
-  if (ev) JJA_CUDA(cudaEventRecord(ev[2], st));
-  launch_levels(p, g, st, false);
+  if (p->dst) {
+    launch_face_solve(p, g, st);
+    if (ev) JJA_CUDA(cudaEventRecord(ev[2], st));
+  } else {
+    launch_levels(p, g, st, true);
+    if (ev) JJA_CUDA(cudaEventRecord(ev[2], st));
+    launch_levels(p, g, st, false);
+  }
   if (ev) JJA_CUDA(cudaEventRecord(ev[3], st));
   if (fuse_next) launch(p->pdl, k_update<true>, grid_for(nj, 256), 256, st, a, p->t, p->xj, (const double*)p->x);
   else launch(p->pdl, k_update<false>, grid_for(nj, 256), 256, st, a, p->t, p->xj, (const double*)p->x);
@@ -1965,6 +2089,7 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->t.inv_c0 = p->up(d->inv_c0, Nj);
     set_face_tables(p->t, ft, [&](auto* h, size_t n) { return p->up(h, n); });
     p->perm = p->up(F.perm.data(), F.perm.size());
+    p->iperm_host.assign(F.iperm.begin(), F.iperm.end());
     {
       const std::vector<longlong2> tab = build_sin_table();
       p->t.sincos = p->up(tab.data(), tab.size());
@@ -2100,6 +2225,65 @@ void jja_plan_destroy(jja_plan* p) { delete p; }
 
 int64_t jja_plan_device_bytes(const jja_plan* p) { return p ? p->bytes : 0; }
 
+int jja_plan_set_fast_poisson(jja_plan* p, int mx, int my, const int32_t* grid_face, double kappa) {
+  return guarded([&] {
+    if (!p || !grid_face || mx < 1 || my < 1) throw Error(JJA_ERR_ARG, "jja_plan_set_fast_poisson: bad arguments");
+    if ((int64_t)mx * my != p->Nf) throw Error(JJA_ERR_ARG, "jja_plan_set_fast_poisson: mx * my != Nf");
+    if (!(kappa > 0.0)) throw Error(JJA_ERR_ARG, "jja_plan_set_fast_poisson: kappa must be positive");
+    auto log2_of = [](int n) {   // log2(2 n) for n a power of two (n = m + 1), else -1
+      if (n < 2 || (n & (n - 1))) return -1;
+      int l = 1;
+      while ((1 << l) < 2 * n) ++l;
+      return l;
+    };
+    const int lgx = log2_of(mx + 1), lgy = log2_of(my + 1);
+    if (lgx < 0 || lgy < 0 || mx + 1 > 1024 || my + 1 > 1024)
+      throw Error(JJA_ERR_ARG, "jja_plan_set_fast_poisson: mx + 1 and my + 1 must be powers of two, at most 1024");
+    std::vector<int32_t> gf((size_t)mx * my);
+    std::vector<char> seen(p->Nf, 0);
+    for (int64_t c = 0; c < (int64_t)mx * my; ++c) {
+      const int f = grid_face[c];
+      if (f < 0 || f >= p->Nf || seen[f]) throw Error(JJA_ERR_ARG, "jja_plan_set_fast_poisson: grid_face is not a permutation");
+      seen[f] = 1;
+      gf[c] = p->iperm_host[f];
+    }
+    const long double pi_l = 3.141592653589793238462643383279502884L;
+    auto twiddles = [&](int m) {
+      const int n = 2 * (m + 1);
+      std::vector<double2> tw(n / 2);
+      for (int k = 0; k < n / 2; ++k)
+        tw[k] = make_double2((double)cosl(2 * pi_l * k / n), (double)-sinl(2 * pi_l * k / n));
+      return tw;
+    };
+    auto eig = [&](int m) {
+      std::vector<double> lam(m);
+      for (int k = 0; k < m; ++k) lam[k] = (double)(2.0L - 2.0L * cosl(pi_l * (k + 1) / (m + 1)));
+      return lam;
+    };
+    DstArgs& d = p->dst_args;
+    d.mx = mx;
+    d.my = my;
+    d.lgx = lgx;
+    d.lgy = lgy;
+    d.grid_face = p->up(gf.data(), gf.size());
+    const std::vector<double2> twx = twiddles(mx), twy = twiddles(my);
+    d.twx = p->up(twx.data(), twx.size());
+    d.twy = p->up(twy.data(), twy.size());
+    const std::vector<double> lx = eig(mx), ly = eig(my);
+    d.lamx = p->up(lx.data(), lx.size());
+    d.lamy = p->up(ly.data(), ly.size());
+    d.scale = (double)((4.0L / ((long double)(mx + 1) * (my + 1))) / kappa);
+    d.t1 = p->up<double>(nullptr, (size_t)p->Nf * p->W);
+    d.t2 = p->up<double>(nullptr, (size_t)p->Nf * p->W);
+    // graphs captured before bake in the sweeps: drop them
+    for (auto& g : p->graphs) cudaGraphExecDestroy(g.exec);
+    for (auto& g : p->adj_graphs) cudaGraphExecDestroy(g.exec);
+    p->graphs.clear();
+    p->adj_graphs.clear();
+    p->dst = 1;
+  });
+}
+
 int jja_plan_test_wait_limit(jja_plan* p, void* stream) {
   return guarded([&] {
     if (!p) throw Error(JJA_ERR_ARG, "jja_plan_test_wait_limit: null plan");
@@ -2153,8 +2337,7 @@ int jja_solve(jja_plan* p, const double* b, double* x, void* stream) {
     const int64_t NfW = (int64_t)p->Nf * p->W;
     k_permute_rows<<<grid_for(NfW, 256), 256, 0, st>>>(b, p->b, p->perm, p->Nf, p->W, 1);
     g_launches++;
-    launch_levels(p, st, true);
-    launch_levels(p, st, false);
+    launch_face_solve(p, st);
     k_permute_rows<<<grid_for(NfW, 256), 256, 0, st>>>(p->x, x, p->perm, p->Nf, p->W, 0);
     g_launches++;
     JJA_CUDA(cudaGetLastError());
@@ -2265,8 +2448,7 @@ static void launch_adjoint_step(jja_plan* p, const AdjArgs& a, cudaStream_t st) 
   s.Nj = p->Nj; s.Nf = p->Nf; s.W = p->W; s.width = p->width; s.w0 = 0; s.wn = p->W; s.d_step = p->all.d_step;
   k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(s, p->t, p->xj, p->b);
   g_launches += 2;
-  launch_levels(p, st, true);
-  launch_levels(p, st, false);
+  launch_face_solve(p, st);
   k_adj_mu<<<grid_for(NjW, 256), 256, 0, st>>>(a, p->t, p->xj, p->x);
   g_launches++;
 }
@@ -2363,8 +2545,7 @@ int jja_adjoint_flux(jja_plan* p, const double* usum, double* gf, void* stream) 
     s.Nj = p->Nj; s.Nf = p->Nf; s.W = p->W; s.width = p->width; s.w0 = 0; s.wn = p->W; s.d_step = p->all.d_step;
     k_face_rhs<<<grid_for(NfW, 256), 256, 0, st>>>(s, p->t, usum, p->b);
     g_launches++;
-    launch_levels(p, st, true);
-    launch_levels(p, st, false);
+    launch_face_solve(p, st);
     k_unpermute_scaled<<<grid_for(NfW, 256), 256, 0, st>>>(p->x, gf, p->perm, p->Nf, p->W, -kTwoPi);
     g_launches++;
     JJA_CUDA(cudaGetLastError());
@@ -2515,8 +2696,14 @@ int jja_run_timed(jja_plan* p, jja_state* s, int nsteps, double* stage_ms, void*
         launch(p->pdl, k_face_rhs, grid_for((int64_t)p->Nf * gs[q]->wn, 256), 256, gst, args[q], p->t,
                (const double*)p->xj, p->b);
       });
-      stage(2, [&](size_t q, cudaStream_t gst) { launch_levels(p, *gs[q], gst, true); });
-      stage(3, [&](size_t q, cudaStream_t gst) { launch_levels(p, *gs[q], gst, false); });
+      // (a fast Poisson plan solves in the "forward" stage; its "backward" stage is empty)
+      stage(2, [&](size_t q, cudaStream_t gst) {
+        if (p->dst) launch_face_solve(p, *gs[q], gst);
+        else launch_levels(p, *gs[q], gst, true);
+      });
+      stage(3, [&](size_t q, cudaStream_t gst) {
+        if (!p->dst) launch_levels(p, *gs[q], gst, false);
+      });
       stage(4, [&](size_t q, cudaStream_t gst) {
         const int64_t nj = (int64_t)p->Nj * gs[q]->wn;
         if (i + 1 < nsteps)

@@ -127,10 +127,49 @@ class HostFactor:
             self.handle = None
 
 
+def fast_poisson_grid(circuit, K):
+    """(mx, my, grid_face, kappa) when the face-space matrix is K = kappa (4 I - adjacency) on an
+    mx x my grid of faces with mx + 1 and my + 1 powers of two (up to 1024): a square array with
+    equal R and C and a uniform self-inductance, whose K is kappa times the 5-point Laplacian with
+    Dirichlet boundaries. Checked entry by entry (relative 1e-12); None otherwise."""
+    try:
+        cx, cy = circuit.get_face_centroids()
+    except Exception:
+        return None
+    Nf = K.shape[0]
+    ux, ix = np.unique(np.round(np.asarray(cx, np.float64), 9), return_inverse=True)
+    uy, iy = np.unique(np.round(np.asarray(cy, np.float64), 9), return_inverse=True)
+    mx, my = len(ux), len(uy)
+    if mx * my != Nf or any(m + 1 > 1024 or (m + 1) & m for m in (mx, my)):
+        return None
+    grid = np.full(mx * my, -1, np.int64)
+    grid[iy * mx + ix] = np.arange(Nf)
+    if np.any(grid < 0):
+        return None
+    Kc = scipy.sparse.coo_matrix(K)
+    kappa = float(K.diagonal()[0]) / 4.0
+    if not kappa > 0.0:
+        return None
+    tol = 1e-12 * kappa
+    if np.abs(K.diagonal() - 4.0 * kappa).max() > tol:
+        return None
+    off = Kc.row != Kc.col
+    r, c, v = Kc.row[off], Kc.col[off], Kc.data[off]
+    neighbour = (np.abs(ix[r] - ix[c]) + np.abs(iy[r] - iy[c])) == 1
+    if not np.all(neighbour) or np.abs(v + kappa).max(initial=0.0) > tol:
+        return None
+    if np.count_nonzero(np.abs(v) > tol) != 2 * (mx * (my - 1) + my * (mx - 1)):
+        return None
+    return mx, my, np.ascontiguousarray(grid, np.int32), kappa
+
+
+FAST_POISSON_MAX_WORK = 1 << 17   # "auto" uses the sine transforms up to this many face-problems (W x Nf)
+
+
 class DevicePlan:
     """Circuit tables + factor uploaded for W problems (owned C object)."""
 
-    def __init__(self, circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=None, tuning=None):
+    def __init__(self, circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=None, tuning=None, fast_poisson=None):
         """``tuning``: dict with any of rhs_block, rows_per_lane, target_warps, min_piece (the
         launch shape of the triangular solves; missing or 0 = library default)."""
         Nj, Nf = circuit._Nj(), circuit._Nf()
@@ -162,6 +201,12 @@ class DevicePlan:
         self.handle = h
         self.Nj, self.Nf, self.W = Nj, Nf, W
         self.inv_c0 = k["inv_c0"]
+        self.fast_poisson = False
+        if fast_poisson is not None:
+            mx, my, grid, kappa = fast_poisson
+            self._keep["grid"] = grid
+            N.check(N.lib().jja_plan_set_fast_poisson(h, int(mx), int(my), N.ptr(grid, ctypes.c_int32), float(kappa)))
+            self.fast_poisson = True
         self.device_bytes = N.lib().jja_plan_device_bytes(h)
 
     def solve(self, b_dev, x_dev, stream=0):
@@ -261,26 +306,31 @@ def get_factor(circuit, dt, nd_leaf=8, ordering="nd", relax=(-1, -1.0)):
 
 
 def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=None, ordering="auto", relax=(-1, -1.0), Ic_w=None,
-             tuning=None):
+             tuning=None, fast_poisson="auto"):
     """Device plan for W problems; ``Ic_w`` (Nj, W) gives each problem its own critical currents;
     ``ordering`` "nd", "mmd" or "auto" (see resolve_ordering); ``nd_leaf`` None: by the step's
     size (see resolve_factor_shape); ``tuning`` the launch shape of the triangular solves (see
-    DevicePlan)."""
+    DevicePlan); ``fast_poisson``: solve with sine transforms when the face-space matrix allows it
+    (fast_poisson_grid): True, False, or "auto" (up to W x Nf = 2^17 face-problems)."""
     ordering = resolve_ordering(ordering, W, circuit._Nf())
     nd_leaf, relax = resolve_factor_shape(nd_leaf, relax, ordering, W, circuit._Nf())
+    fp = None
+    if fast_poisson is True or (fast_poisson == "auto" and W * circuit._Nf() <= FAST_POISSON_MAX_WORK):
+        fp = fast_poisson_grid(circuit, face_matrix(circuit, dt)[1])
     factor, A, fkey = get_factor(circuit, dt, nd_leaf, ordering=ordering, relax=relax)
     Rv, Cv, coef = coefficients(circuit, dt, stencil)
     if Ic_w is not None:
         Ic_w = np.ascontiguousarray(np.broadcast_to(np.asarray(Ic_w, np.float64), (circuit._Nj(), W)))
     ic = np.asarray(circuit._Ic(), np.float64) if Ic_w is None else Ic_w
     tkey = tuple(int((tuning or {}).get(f, 0)) for f in TUNING_FIELDS)
-    key = (fkey, W, stencil_width, Ic_w is None, tkey, _digest(ic, *coef, Rv, A.indptr, A.indices, A.data))
+    key = (fkey, W, stencil_width, Ic_w is None, tkey, fp is not None,
+           _digest(ic, *coef, Rv, A.indptr, A.indices, A.data))
     with _CACHE_LOCK:
         p = _PLANS.get(key)
         if p is not None:
             _PLANS.move_to_end(key)
             return p
-    p = DevicePlan(circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=Ic_w, tuning=tuning)
+    p = DevicePlan(circuit, factor, A, W, dt, stencil_width, stencil, Ic_w=Ic_w, tuning=tuning, fast_poisson=fp)
     with _CACHE_LOCK:
         _PLANS[key] = p
         while len(_PLANS) > MAX_PLANS:
