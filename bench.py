@@ -235,9 +235,10 @@ def ac_driven_leg(G, torch, Nt, parity_steps=200):
     # host fills the next window of the callable's values while the GPU runs the current one)
     from pyjjasim_gb300.backend import GpuSimulation
     dev = {}
-    for mode, tuning in (("levels", None), ("levels_pdl", {"pdl": 1}), ("dataflow", {"schedule": 2}),
-                         ("dataflow_pdl", {"schedule": 2, "pdl": 1})):
-        sim = GpuSimulation(problem(4096, [4095]), seed=2, tuning=tuning)
+    for mode, kw in (("fast_poisson", dict(fast_poisson=True)), ("sweeps", dict(fast_poisson=False)),
+                     ("sweeps_pdl", dict(fast_poisson=False, tuning={"pdl": 1})),
+                     ("sweeps_dataflow", dict(fast_poisson=False, tuning={"schedule": 2}))):
+        sim = GpuSimulation(problem(4096, [4095]), seed=2, **kw)
         dev[mode] = _timed_steps(torch, sim, 2048) / 2048 * 1e3
         del sim
     best = min(dev, key=dev.get)
@@ -763,21 +764,31 @@ def main():
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s"},
             "stage_ms_per_step": {k: v / args.steps for k, v in stages.items()},
             "stage_share": stage_share}
-        # plain GPU path: one problem per launch, in its fastest launch mode (programmatic
-        # dependent launch pays off for its short kernels; the default launch is reported beside)
+        # plain GPU path: one problem per launch. (a) The batched path's own solver (supernodal
+        # sweeps) at W = 1 in its fastest launch mode: the batching ratio. (b) The library's
+        # fastest W = 1 path, the sine-transform face solve this uniform square array allows.
         prob1 = make_problem(G, 1, [1.0])
         k1 = max(args.steps, 200)
         plain_ms = {}
         for mode, tuning in (("pdl", {"pdl": 1}), ("default", None), ("dataflow", {"schedule": 2}),
-                             ("dataflow_pdl", {"schedule": 2, "pdl": 1})):
-            sim1 = GpuSimulation(prob1, tuning=tuning, **factor_opts(args))
+                             ("cooperative", {"schedule": 3})):
+            sim1 = GpuSimulation(prob1, tuning=tuning, fast_poisson=False, **factor_opts(args))
             t1 = _timed_steps(torch, sim1, k1)
             plain_ms[mode] = t1 / k1 * 1e3
             del sim1
         t1 = min(plain_ms.values()) * k1 / 1e3
         plain = Nj * k1 / t1
+        sim1 = GpuSimulation(prob1, fast_poisson=True, **factor_opts(args))
+        t_fp = _timed_steps(torch, sim1, k1)
+        del sim1
+        fp = Nj * k1 / t_fp
         line["plain_gpu"] = {"value": plain, "unit": "junction-steps/s", "W": 1, "ms_per_step": t1 / k1 * 1e3,
-                             "ms_per_step_by_launch_mode": plain_ms, "batched_over_plain": value / world / plain}
+                             "solver": "supernodal sweeps (the batched path's solver)",
+                             "ms_per_step_by_launch_mode": plain_ms, "batched_over_plain": value / world / plain,
+                             "fast_poisson": {"value": fp, "ms_per_step": t_fp / k1 * 1e3,
+                                              "solver": "sine transforms (uniform square array), the library's "
+                                                        "default at W = 1",
+                                              "batched_over_plain": value / world / fp}}
         # end to end through the public API with host buffers: the workload as a user runs it,
         # Ne steps with steps Ne/2-1 and Ne-1 stored, the IV-curve point read from them on the
         # host (config: 10000 steps, the first 5000 discarded). Cold: the first call on an empty

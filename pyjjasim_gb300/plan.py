@@ -163,7 +163,12 @@ def fast_poisson_grid(circuit, K):
     return mx, my, np.ascontiguousarray(grid, np.int32), kappa
 
 
-FAST_POISSON_MAX_WORK = 1 << 17   # "auto" uses the sine transforms up to this many face-problems (W x Nf)
+# "auto" uses the sine transforms for at most this many problems and face-problems (W x Nf). Measured
+# on GB300 (device ms per step, transforms / sweeps): 256x256 W = 1 0.066 / 0.158, 128x128 W = 1
+# 0.031 / 0.082, W = 8 0.092 / 0.142, W = 16 0.168 / 0.163, W = 64 0.60 / 0.30; 512x512 W = 1
+# 0.23 / 0.36; 1024x1024 W = 1 0.85 / 0.79, W = 8 6.3 / 2.9; 64x64 W = 64 0.150 / 0.129
+FAST_POISSON_MAX_W = 8
+FAST_POISSON_MAX_WORK = 1 << 18
 
 
 class DevicePlan:
@@ -311,11 +316,12 @@ def get_plan(circuit, dt, W, stencil_width, stencil, nd_leaf=None, ordering="aut
     ``ordering`` "nd", "mmd" or "auto" (see resolve_ordering); ``nd_leaf`` None: by the step's
     size (see resolve_factor_shape); ``tuning`` the launch shape of the triangular solves (see
     DevicePlan); ``fast_poisson``: solve with sine transforms when the face-space matrix allows it
-    (fast_poisson_grid): True, False, or "auto" (up to W x Nf = 2^17 face-problems)."""
+    (fast_poisson_grid): True, False, or "auto" (W <= 8 and W x Nf <= 2^18 face-problems)."""
     ordering = resolve_ordering(ordering, W, circuit._Nf())
     nd_leaf, relax = resolve_factor_shape(nd_leaf, relax, ordering, W, circuit._Nf())
     fp = None
-    if fast_poisson is True or (fast_poisson == "auto" and W * circuit._Nf() <= FAST_POISSON_MAX_WORK):
+    if fast_poisson is True or (fast_poisson == "auto" and W <= FAST_POISSON_MAX_W
+                                and W * circuit._Nf() <= FAST_POISSON_MAX_WORK):
         fp = fast_poisson_grid(circuit, face_matrix(circuit, dt)[1])
     factor, A, fkey = get_factor(circuit, dt, nd_leaf, ordering=ordering, relax=relax)
     Rv, Cv, coef = coefficients(circuit, dt, stencil)
