@@ -69,3 +69,28 @@ def test_mismatched_problems_rejected():
 def test_ragged_batch_on_gpu(parts):
     problems = _problems()
     _check(RaggedBatch(problems, parts=parts).compute(), problems, rtol=1e-9)
+
+
+@pytest.mark.gpu
+def test_three_part_batch_of_all_lattices_against_the_oracle():
+    """Six problems, square / honeycomb / triangular at sides 64-80 (about 140k junctions), run
+    as three concurrent parts (each its own union, factor and stream); every problem against the
+    oracle run alone: phases 1e-9 relative, vortex configurations equal."""
+    Nt = 120
+    specs = [(SquareArray, 64, 0.6), (HoneycombArray, 64, 1.1), (TriangularArray, 70, 0.9), (SquareArray, 80, 1.5),
+             (HoneycombArray, 66, 0.4), (TriangularArray, 64, 1.3)]
+    problems = []
+    for cls, n, b in specs:
+        c = cls(n, n)
+        Is = c.current_base(0.0)[:, None, None] * np.array([b])[None, :, None]
+        problems.append(TimeEvolutionProblem(c, time_step=0.05, time_step_count=Nt, current_sources=Is,
+                                             external_flux=0.2, store_time_steps=[Nt // 2, Nt - 1],
+                                             store_current=False, store_voltage=False))
+    batch = RaggedBatch(problems, parts=3)
+    assert len(batch.parts) == 3
+    for res, p in zip(batch.compute(), problems):
+        th, _, _ = rcsj_oracle.time_evolution(p)
+        scale = max(1.0, float(np.abs(th).max()))
+        assert float(np.abs(res.get_theta() - th).max()) <= 1e-9 * scale
+        assert np.array_equal(res.get_vortex_configuration(),
+                              rcsj_oracle.vortex_configuration(p.get_circuit().get_cycle_matrix(), th))
