@@ -611,6 +611,31 @@ def profile_mode(args):
     import pyjjasim_gb300 as G
     from pyjjasim_gb300.backend import GpuSimulation
     torch.cuda.set_device(0)
+    if args.profile_case == "fast_poisson":
+        # the AC-driven single array's solver: SquareArray(256,256), C = 1, L = 0.1, W = 1, whose
+        # face solves are the three sine-transform kernels (k_dst_rows, k_dst_cols, k_dst_rows)
+        a = G.SquareArray(256, 256)
+        a.set_capacitance(1.0)
+        a.set_inductance(0.1)
+        p = G.TimeEvolutionProblem(a, time_step=0.05, time_step_count=10 ** 6, external_flux=0.1,
+                                   current_sources=0.8 * a.current_base(0.0)[:, None, None])
+        sim = GpuSimulation(p, fast_poisson=True)
+        sim.run(3 + args.profile_steps, use_graph=False)
+        sim.synchronize()
+        ok = bool(sim.plan.fast_poisson) and bool(torch.isfinite(sim.theta()).all())
+        print(json.dumps({"profile_case": "fast_poisson", "steps": 3 + args.profile_steps, "ok": ok}))
+        sys.exit(0 if ok else 1)
+    if args.profile_case == "static":
+        # the static solver's refactorisation: 64 problems on SquareArray(64,64), L = 0.1
+        from pyjjasim_gb300.static import StaticProblem, compute_many
+        a = G.SquareArray(64, 64)
+        a.set_inductance(0.1)
+        probs = [StaticProblem(a, current_sources=(0.05 + 0.05 * (w % 6)) * a.current_base(0.05 * w))
+                 for w in range(64)]
+        out = compute_many(probs)
+        ok = sum(st == 0 for _, st, _ in out) > 0
+        print(json.dumps({"profile_case": "static", "problems": 64, "converged": int(sum(st == 0 for _, st, _ in out))}))
+        sys.exit(0 if ok else 1)
     prob = make_problem(G, 1, np.linspace(0.0, 2.0, args.W))
     sim = GpuSimulation(prob, **factor_opts(args))
     sim.run(3, use_graph=False)
@@ -633,6 +658,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-case", default="iv", choices=["iv", "fast_poisson", "static"],
+                    help="profiling mode: the IV sweep (default), the fast Poisson single array, the static solver")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling mode: plan, 3 eager warm-up steps, then this many eager steps, nothing else")
     ap.add_argument("--W", type=int, default=W_BATCH, help="problems per launch (profiling mode)")

@@ -1005,16 +1005,23 @@ struct DstArgs {
   double* t2;
 };
 
-// load the odd extension of x (m values at x[j * stride]) into a (bit-reversed order), then
-// transform; on return -Im(a[k]) / 2, k = 1..m, is the DST-I of x
-__device__ __forceinline__ void dst_line(double2* a, const double* x, int64_t stride, int m, int lg,
+// Two lines per transform: z = e1 + i e2 for the odd extensions e1, e2 of x1 and x2 (m values
+// each at x[j * stride]; x2 may be null), loaded in bit-reversed order and transformed in place.
+// As e1 and e2 are real, the DST-I of x1 is -(Im Z_k - Im Z_{n-k}) / 4 and that of x2 is
+// (Re Z_k - Re Z_{n-k}) / 4, k = 1..m (dst_pair_out): half the butterflies of one FFT per line.
+__device__ __forceinline__ void dst_pair(double2* a, const double* x1, const double* x2, int64_t stride, int m, int lg,
                                          const double2* __restrict__ tw) {
   const int n = 2 * (m + 1), N = m + 1;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    double e = 0.0;
-    if (i >= 1 && i <= m) e = x[(int64_t)(i - 1) * stride];
-    else if (i > N) e = -x[(int64_t)(n - i - 1) * stride];
-    a[__brev((unsigned)i) >> (32 - lg)] = make_double2(e, 0.0);
+    double e1 = 0.0, e2 = 0.0;
+    if (i >= 1 && i <= m) {
+      e1 = x1[(int64_t)(i - 1) * stride];
+      if (x2) e2 = x2[(int64_t)(i - 1) * stride];
+    } else if (i > N) {
+      e1 = -x1[(int64_t)(n - i - 1) * stride];
+      if (x2) e2 = -x2[(int64_t)(n - i - 1) * stride];
+    }
+    a[__brev((unsigned)i) >> (32 - lg)] = make_double2(e1, e2);
   }
   __syncthreads();
   for (int l = 1; l <= lg; ++l) {
@@ -1032,48 +1039,71 @@ __device__ __forceinline__ void dst_line(double2* a, const double* x, int64_t st
   }
 }
 
-// rows: out(w, iy, k) = DST_x of row iy of problem w0 + blockIdx.y; `in_faces`: the input is a
-// face vector (N x W, factor's face order) read through grid_face, else a (W, my, mx) scratch;
-// `out_faces` likewise for the output
+// the two lines' DST-I values at k = 1..m from the transformed buffer
+__device__ __forceinline__ double2 dst_pair_out(const double2* a, int n, int k) {
+  const double2 zk = a[k], zn = a[n - k];
+  return make_double2(-0.25 * (zk.y - zn.y), 0.25 * (zk.x - zn.x));
+}
+
+// rows: out(w, iy, k) = DST_x of rows iy = 2 blockIdx.x and 2 blockIdx.x + 1 of problem
+// w0 + blockIdx.y; `in_faces`: the input is a face vector (N x W, factor's face order) read
+// through grid_face, else a (W, my, mx) scratch; `out_faces` likewise for the output
 __global__ void k_dst_rows(DstArgs d, const double* in, double* out, int W, int w0, int in_faces, int out_faces) {
   extern __shared__ double2 fft_buf[];
-  const int iy = blockIdx.x, w = w0 + blockIdx.y;
-  const double* src;
-  int64_t stride;
+  const int iy0 = 2 * blockIdx.x, iy1 = iy0 + 1, w = w0 + blockIdx.y, n = 2 * (d.mx + 1);
+  const bool two = iy1 < d.my;
+  const double *src0, *src1 = nullptr;
   if (in_faces) {
-    // gather the row through the face map into the tail of the buffer's real parts first
-    double* row = reinterpret_cast<double*>(fft_buf + 2 * (d.mx + 1));
-    for (int j = threadIdx.x; j < d.mx; j += blockDim.x) row[j] = in[(int64_t)__ldg(d.grid_face + iy * d.mx + j) * W + w];
+    // gather both rows through the face map after the FFT buffer
+    double* rows = reinterpret_cast<double*>(fft_buf + n);
+    for (int j = threadIdx.x; j < d.mx; j += blockDim.x) {
+      rows[j] = in[(int64_t)__ldg(d.grid_face + iy0 * d.mx + j) * W + w];
+      if (two) rows[d.mx + j] = in[(int64_t)__ldg(d.grid_face + iy1 * d.mx + j) * W + w];
+    }
     __syncthreads();
-    src = row;
-    stride = 1;
+    src0 = rows;
+    if (two) src1 = rows + d.mx;
   } else {
-    src = in + ((int64_t)w * d.my + iy) * d.mx;
-    stride = 1;
+    src0 = in + ((int64_t)w * d.my + iy0) * d.mx;
+    if (two) src1 = src0 + d.mx;
   }
-  dst_line(fft_buf, src, stride, d.mx, d.lgx, d.twx);
+  dst_pair(fft_buf, src0, src1, 1, d.mx, d.lgx, d.twx);
   for (int k = threadIdx.x; k < d.mx; k += blockDim.x) {
-    const double y = -0.5 * fft_buf[k + 1].y;
-    if (out_faces) out[(int64_t)__ldg(d.grid_face + iy * d.mx + k) * W + w] = y;
-    else out[((int64_t)w * d.my + iy) * d.mx + k] = y;
+    const double2 y = dst_pair_out(fft_buf, n, k + 1);
+    if (out_faces) {
+      out[(int64_t)__ldg(d.grid_face + iy0 * d.mx + k) * W + w] = y.x;
+      if (two) out[(int64_t)__ldg(d.grid_face + iy1 * d.mx + k) * W + w] = y.y;
+    } else {
+      out[((int64_t)w * d.my + iy0) * d.mx + k] = y.x;
+      if (two) out[((int64_t)w * d.my + iy1) * d.mx + k] = y.y;
+    }
   }
 }
 
-// columns: DST_y, division by the eigenvalues times the scale, inverse DST_y (DST-I is its own
-// inverse up to the scale)
+// columns kx = 2 blockIdx.x and 2 blockIdx.x + 1: DST_y, division by the eigenvalues times the
+// scale, inverse DST_y (DST-I is its own inverse up to the scale)
 __global__ void k_dst_cols(DstArgs d, int w0) {
   extern __shared__ double2 fft_buf[];
-  const int kx = blockIdx.x, w = w0 + blockIdx.y;
-  const double* col = d.t1 + (int64_t)w * d.my * d.mx + kx;
-  double* tmp = reinterpret_cast<double*>(fft_buf + 2 * (d.my + 1));   // my values after the FFT buffer
-  dst_line(fft_buf, col, d.mx, d.my, d.lgy, d.twy);
-  const double lx = __ldg(d.lamx + kx);
-  for (int k = threadIdx.x; k < d.my; k += blockDim.x)
-    tmp[k] = -0.5 * fft_buf[k + 1].y * d.scale / (lx + __ldg(d.lamy + k));
+  const int kx0 = 2 * blockIdx.x, kx1 = kx0 + 1, w = w0 + blockIdx.y, n = 2 * (d.my + 1);
+  const bool two = kx1 < d.mx;
+  const double* col = d.t1 + (int64_t)w * d.my * d.mx + kx0;
+  double* tmp = reinterpret_cast<double*>(fft_buf + n);   // 2 x my values after the FFT buffer
+  dst_pair(fft_buf, col, two ? col + 1 : nullptr, d.mx, d.my, d.lgy, d.twy);
+  const double lx0 = __ldg(d.lamx + kx0), lx1 = two ? __ldg(d.lamx + kx1) : 0.0;
+  for (int k = threadIdx.x; k < d.my; k += blockDim.x) {
+    const double2 y = dst_pair_out(fft_buf, n, k + 1);
+    const double ly = __ldg(d.lamy + k);
+    tmp[k] = y.x * d.scale / (lx0 + ly);
+    tmp[d.my + k] = two ? y.y * d.scale / (lx1 + ly) : 0.0;
+  }
   __syncthreads();
-  dst_line(fft_buf, tmp, 1, d.my, d.lgy, d.twy);
-  double* out = d.t2 + (int64_t)w * d.my * d.mx + kx;
-  for (int k = threadIdx.x; k < d.my; k += blockDim.x) out[(int64_t)k * d.mx] = -0.5 * fft_buf[k + 1].y;
+  dst_pair(fft_buf, tmp, two ? tmp + d.my : nullptr, 1, d.my, d.lgy, d.twy);
+  double* out = d.t2 + (int64_t)w * d.my * d.mx + kx0;
+  for (int k = threadIdx.x; k < d.my; k += blockDim.x) {
+    const double2 y = dst_pair_out(fft_buf, n, k + 1);
+    out[(int64_t)k * d.mx] = y.x;
+    if (two) out[(int64_t)k * d.mx + 1] = y.y;
+  }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1779,12 +1809,14 @@ void launch_face_solve(jja_plan* p, const Group& g, cudaStream_t st) {
     return;
   }
   const DstArgs& d = p->dst_args;
-  const size_t smx = (size_t)2 * (d.mx + 1) * sizeof(double2) + (size_t)d.mx * sizeof(double);
-  const size_t smy = (size_t)2 * (d.my + 1) * sizeof(double2) + (size_t)d.my * sizeof(double);
+  // an FFT buffer of 2 (m + 1) complex points, then two lines of m values
+  const size_t smx = (size_t)2 * (d.mx + 1) * sizeof(double2) + (size_t)2 * d.mx * sizeof(double);
+  const size_t smy = (size_t)2 * (d.my + 1) * sizeof(double2) + (size_t)2 * d.my * sizeof(double);
   const int tx = std::min(512, d.mx + 1), ty = std::min(512, d.my + 1);
-  k_dst_rows<<<dim3((unsigned)d.my, (unsigned)g.wn), tx, smx, st>>>(d, p->b, d.t1, p->W, g.w0, 1, 0);
-  k_dst_cols<<<dim3((unsigned)d.mx, (unsigned)g.wn), ty, smy, st>>>(d, g.w0);
-  k_dst_rows<<<dim3((unsigned)d.my, (unsigned)g.wn), tx, smx, st>>>(d, d.t2, p->x, p->W, g.w0, 0, 1);
+  const unsigned row_pairs = (unsigned)((d.my + 1) / 2), col_pairs = (unsigned)((d.mx + 1) / 2);
+  k_dst_rows<<<dim3(row_pairs, (unsigned)g.wn), tx, smx, st>>>(d, p->b, d.t1, p->W, g.w0, 1, 0);
+  k_dst_cols<<<dim3(col_pairs, (unsigned)g.wn), ty, smy, st>>>(d, g.w0);
+  k_dst_rows<<<dim3(row_pairs, (unsigned)g.wn), tx, smx, st>>>(d, d.t2, p->x, p->W, g.w0, 0, 1);
   g_launches += 3;
 }
 
