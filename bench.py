@@ -235,7 +235,10 @@ def ac_driven_leg(G, torch, Nt, parity_steps=200):
     # host fills the next window of the callable's values while the GPU runs the current one)
     from pyjjasim_gb300.backend import GpuSimulation
     dev = {}
-    for mode, kw in (("fast_poisson", dict(fast_poisson=True)), ("sweeps", dict(fast_poisson=False)),
+    for mode, kw in (("fast_poisson", dict(fast_poisson=True)),
+                     ("fast_poisson_1line", dict(fast_poisson=True, tuning={"dst_lines": 1})),
+                     ("fast_poisson_2lines", dict(fast_poisson=True, tuning={"dst_lines": 2})),
+                     ("sweeps", dict(fast_poisson=False)),
                      ("sweeps_pdl", dict(fast_poisson=False, tuning={"pdl": 1})),
                      ("sweeps_dataflow", dict(fast_poisson=False, tuning={"schedule": 2}))):
         sim = GpuSimulation(problem(4096, [4095]), seed=2, **kw)
@@ -805,9 +808,12 @@ def main():
             del sim1
         t1 = min(plain_ms.values()) * k1 / 1e3
         plain = Nj * k1 / t1
-        sim1 = GpuSimulation(prob1, fast_poisson=True, **factor_opts(args))
-        t_fp = _timed_steps(torch, sim1, k1)
-        del sim1
+        fp_ms = {}
+        for mode, tuning in (("default", None), ("1line", {"dst_lines": 1}), ("2lines", {"dst_lines": 2})):
+            sim1 = GpuSimulation(prob1, fast_poisson=True, tuning=tuning, **factor_opts(args))
+            fp_ms[mode] = _timed_steps(torch, sim1, k1) / k1 * 1e3
+            del sim1
+        t_fp = fp_ms["default"] * k1 / 1e3
         fp = Nj * k1 / t_fp
         line["plain_gpu"] = {"value": plain, "unit": "junction-steps/s", "W": 1, "ms_per_step": t1 / k1 * 1e3,
                              "solver": "supernodal sweeps (the batched path's solver)",
@@ -815,6 +821,7 @@ def main():
                              "fast_poisson": {"value": fp, "ms_per_step": t_fp / k1 * 1e3,
                                               "solver": "sine transforms (uniform square array), the library's "
                                                         "default at W = 1",
+                                              "ms_per_step_by_lines_per_block": fp_ms,
                                               "batched_over_plain": value / world / fp}}
         # end to end through the public API with host buffers: the workload as a user runs it,
         # Ne steps with steps Ne/2-1 and Ne-1 stored, the IV-curve point read from them on the

@@ -106,6 +106,14 @@ typedef struct {
                          0: default (W / 160 clamped to [2, 4] from W = 256 on, else 1) */
   int coop_blocks;    /* cooperative schedule: at most this many blocks per sweep launch (0: two per
                          SM, fewer when the widest level has fewer work items) */
+  int dst_lines;      /* fast Poisson solve (jja_plan_set_fast_poisson): grid lines per block of the
+                         sine-transform kernels, 1 or 2 (two real lines share one complex FFT);
+                         0: default (2 when that still gives at least 2 x 152 blocks, else 1) */
+  int subtree_rows;   /* level schedule with 32 problems per warp (W >= 17): subtrees at the bottom of
+                         the elimination tree spanning at most this many rows (their columns plus
+                         their root's off-diagonal rows, <= 64) are solved one warp per subtree and
+                         32 problems in shared memory, one launch per sweep, before the levels
+                         above them; 0: default (32); negative: never */
 } jja_solve_tuning;
 
 /* Builds on the host (no GPU needed) the work-item schedule that jja_plan_create would make for

@@ -76,8 +76,14 @@ constexpr int kPackMaxK = 8;           // ... and at most this many columns
 constexpr int kDefaultPackMinWarps = 152 * 64 * 2;   // ... on levels with at least two waves of warps
 constexpr int kGroupsFromW = 256;      // from this many problems the step runs as concurrent groups ...
 constexpr int kGroupW = 160;           // ... of about this many problems, 2 to 4 of them
+constexpr int kNumSMs = 152;                     // GB300
 constexpr int kDefaultTargetWarps = 152 * 24;   // levels with fewer work items split their dot products
 constexpr int kDefaultMinPiece = 16;     // shortest piece of a split dot product
+constexpr int kDefaultSubRows = 32;     // subtree sweeps: rows per subtree (columns + the root's off-diagonal rows)
+constexpr int kSubMaxWarps = 8;         // ... warps (32-problem blocks of one subtree) per block
+constexpr int kSubMaxK = 8;             // ... members of at most this many columns
+constexpr int kSubMaxF = 2048;          // ... at most this many F values per subtree
+constexpr int kSubMaxL = 4096;          // ... at most this many off-diagonal entries per subtree
 constexpr int kUnroll = JJA_UNROLL;   // columns whose loads are issued ahead of their FMAs
 constexpr double kTwoPi = 6.283185307179586;
 constexpr int kEllMax = 6;          // faces with up to 6 junctions (square 4, triangular 3, honeycomb 6)
@@ -831,6 +837,182 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_bwd_level(FactorDev F, 
 }
 
 // ------------------------------------------------------------------------------------------
+// Subtree sweeps (level schedule, 32 problems per warp). The bottom of the elimination tree is
+// cut into subtrees of at most a few dozen rows: a subtree's columns are contiguous (postorder),
+// every row outside it that a member touches is an off-diagonal row of its root (the structure
+// of a column is contained in its parent's), so one warp can solve a whole subtree for its 32
+// problems with the subtree's rows in shared memory: lane = problem, rows [0, ncols) are the
+// subtree's columns, rows [ncols, ncols + m_root) the root's off-diagonal rows. Each lane walks
+// the members in postorder (forward) or reverse postorder (backward) on its own column of that
+// buffer, so no lane waits for another; the block's warps (consecutive 32-problem blocks of the
+// same subtree) share the members' F values, staged once. This replaces the bottom levels'
+// launches, their per-item index loads and the scatter atomics inside the subtree: one atomic per
+// (outside row, problem) remains, and every row of b, z and x the subtree owns moves once.
+// ------------------------------------------------------------------------------------------
+struct SubTree {
+  int s0, n;             // first member supernode, member count (the root is s0 + n - 1)
+  int c0, ncols;         // first column, column count
+  int m_root;            // the root's off-diagonal row count
+  int f_len, l_len;      // the members' F values (row-major), entries of their local row maps
+  int pad;
+  int64_t f_off, l_off, r_off;   // into frow, the local row maps, and rows (the root's)
+};
+
+struct SubDev {
+  const SubTree* tab = nullptr;
+  const int4* meta = nullptr;      // per member supernode: column - c0, k, k + m, F offset - f_off
+  const int32_t* lrow = nullptr;   // per member supernode: offset of its local row map - l_off
+  const uint16_t* loc = nullptr;   // local row (in the subtree buffer) of every off-diagonal row
+  int n = 0;                       // subtrees
+  int max_rows = 0, max_f = 0, max_n = 0, max_l = 0;   // largest per subtree (max_f even)
+};
+
+// dynamic shared memory of a subtree launch with `warps` warps per block: the warps' row
+// buffers, then F values, member metadata, local row map offsets and the local row maps
+__host__ __device__ inline size_t sub_smem_bytes(const SubDev& S, int warps) {
+  return (size_t)warps * S.max_rows * 32 * sizeof(double) + (size_t)S.max_f * sizeof(double) +
+         (size_t)S.max_n * (sizeof(int4) + sizeof(int32_t)) + (size_t)S.max_l * sizeof(uint16_t);
+}
+
+// forward, one member with K columns: z rows from the buffer's b rows, then its off-diagonal
+// rows updated in the buffer (b_R -= F21 b_s). `buf` points at this lane's row 0 (rows 32
+// doubles apart), `zs` at z row c0 + c of this lane's problem.
+template <int K>
+__device__ __forceinline__ void sub_fwd_member(const double* Fr, const uint16_t* L, int c, int nf, double* buf,
+                                               double* zs, int64_t W) {
+  double bs[K];
+#pragma unroll
+  for (int j = 0; j < K; ++j) bs[j] = buf[(c + j) * 32];
+#pragma unroll
+  for (int r = 0; r < K; ++r) {
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j <= r; ++j) acc = fma(Fr[r * K + j], bs[j], acc);
+    zs[(int64_t)r * W] = acc;
+  }
+  // two rows at a time: a member's off-diagonal rows are distinct, so both loads go first
+  int r = K;
+  for (; r + 2 <= nf; r += 2) {
+    const int l0 = L[r - K], l1 = L[r + 1 - K];
+    double t0 = buf[l0 * 32], t1 = buf[l1 * 32];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      t0 = fma(-Fr[r * K + j], bs[j], t0);
+      t1 = fma(-Fr[(r + 1) * K + j], bs[j], t1);
+    }
+    buf[l0 * 32] = t0;
+    buf[l1 * 32] = t1;
+  }
+  if (r < nf) {
+    const int l0 = L[r - K];
+    double t0 = buf[l0 * 32];
+#pragma unroll
+    for (int j = 0; j < K; ++j) t0 = fma(-Fr[r * K + j], bs[j], t0);
+    buf[l0 * 32] = t0;
+  }
+}
+
+// backward, one member: x_s = inv(L11)^T z_s - (L21 inv(L11))^T x_R with z_s in the buffer's
+// own rows and x_R in its ancestors' rows (computed before, or loaded for the root's rows);
+// x_s replaces z_s in the buffer and goes to x row c0 + c (`xs`)
+template <int K>
+__device__ __forceinline__ void sub_bwd_member(const double* Fr, const uint16_t* L, int c, int nf, double* buf,
+                                               double* xs, int64_t W) {
+  double acc[K];
+#pragma unroll
+  for (int j = 0; j < K; ++j) acc[j] = 0.0;
+#pragma unroll
+  for (int r = 0; r < K; ++r) {
+    const double zr = buf[(c + r) * 32];
+#pragma unroll
+    for (int j = 0; j <= r; ++j) acc[j] = fma(Fr[r * K + j], zr, acc[j]);
+  }
+#pragma unroll 4
+  for (int r = K; r < nf; ++r) {
+    const double xr = buf[L[r - K] * 32];
+#pragma unroll
+    for (int j = 0; j < K; ++j) acc[j] = fma(-Fr[r * K + j], xr, acc[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    buf[(c + j) * 32] = acc[j];
+    xs[(int64_t)j * W] = acc[j];
+  }
+}
+
+// grid (subtrees, ceil(problem blocks / warps per block)); block = warps per block x 32.
+// Forward: b rows in, z rows out, the root's off-diagonal rows of b updated atomically.
+// Backward: z rows and the root's off-diagonal rows of x in, x rows out.
+template <bool kForward>
+__global__ void __launch_bounds__(256) k_subtree(FactorDev F, SubDev S, int W, int w0, int wn,
+                                                 double* __restrict__ b, double* __restrict__ z,
+                                                 double* __restrict__ x) {
+  pdl_begin();
+  extern __shared__ double sub_sh[];
+  const SubTree T = S.tab[blockIdx.x];
+  const int nw = blockDim.x >> 5, wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* Fsh = sub_sh + (size_t)nw * S.max_rows * 32;
+  int4* Msh = reinterpret_cast<int4*>(Fsh + S.max_f);
+  int32_t* Lrow = reinterpret_cast<int32_t*>(Msh + S.max_n);
+  uint16_t* Lsh = reinterpret_cast<uint16_t*>(Lrow + S.max_n);
+  for (int i = threadIdx.x; i < T.f_len; i += blockDim.x) Fsh[i] = __ldg(F.frow + T.f_off + i);
+  for (int i = threadIdx.x; i < T.n; i += blockDim.x) {
+    Msh[i] = __ldg(S.meta + T.s0 + i);
+    Lrow[i] = __ldg(S.lrow + T.s0 + i);
+  }
+  for (int i = threadIdx.x; i < T.l_len; i += blockDim.x) Lsh[i] = __ldg(S.loc + T.l_off + i);
+  __syncthreads();
+  const int w = w0 + (blockIdx.y * nw + wi) * 32 + lane;
+  if (w >= w0 + wn || w >= W) return;
+  double* buf = sub_sh + (size_t)wi * S.max_rows * 32 + lane;
+  const int32_t* R = F.rows + T.r_off;
+  const int64_t Wl = W;
+  if (kForward) {
+#pragma unroll 4
+    for (int i = 0; i < T.ncols; ++i) buf[i * 32] = b[(int64_t)(T.c0 + i) * Wl + w];
+    for (int q = 0; q < T.m_root; ++q) buf[(T.ncols + q) * 32] = 0.0;
+    for (int i = 0; i < T.n; ++i) {
+      const int4 mt = Msh[i];
+      const double* Fr = Fsh + mt.w;
+      const uint16_t* L = Lsh + Lrow[i];
+      double* zs = z + (int64_t)(T.c0 + mt.x) * Wl + w;
+      switch (mt.y) {
+        case 1: sub_fwd_member<1>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
+        case 2: sub_fwd_member<2>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
+        case 3: sub_fwd_member<3>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
+        case 4: sub_fwd_member<4>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
+        case 5: sub_fwd_member<5>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
+        case 6: sub_fwd_member<6>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
+        case 7: sub_fwd_member<7>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
+        default: sub_fwd_member<8>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
+      }
+    }
+    for (int q = 0; q < T.m_root; ++q) atomicAdd(b + (int64_t)__ldg(R + q) * Wl + w, buf[(T.ncols + q) * 32]);
+  } else {
+#pragma unroll 4
+    for (int q = 0; q < T.m_root; ++q) buf[(T.ncols + q) * 32] = __ldcg(x + (int64_t)__ldg(R + q) * Wl + w);
+#pragma unroll 4
+    for (int i = 0; i < T.ncols; ++i) buf[i * 32] = __ldg(z + (int64_t)(T.c0 + i) * Wl + w);
+    for (int i = T.n - 1; i >= 0; --i) {
+      const int4 mt = Msh[i];
+      const double* Fr = Fsh + mt.w;
+      const uint16_t* L = Lsh + Lrow[i];
+      double* xs = x + (int64_t)(T.c0 + mt.x) * Wl + w;
+      switch (mt.y) {
+        case 1: sub_bwd_member<1>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
+        case 2: sub_bwd_member<2>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
+        case 3: sub_bwd_member<3>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
+        case 4: sub_bwd_member<4>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
+        case 5: sub_bwd_member<5>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
+        case 6: sub_bwd_member<6>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
+        case 7: sub_bwd_member<7>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
+        default: sub_bwd_member<8>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
 // Dataflow sweeps: ONE launch per sweep. Warps take items in the sweep's topological order from
 // a global counter; an item starts once the items it depends on have finished, which is
 // tracked by per-supernode completion counters instead of a kernel boundary per level:
@@ -1010,7 +1192,7 @@ struct DstArgs {
 // As e1 and e2 are real, the DST-I of x1 is -(Im Z_k - Im Z_{n-k}) / 4 and that of x2 is
 // (Re Z_k - Re Z_{n-k}) / 4, k = 1..m (dst_pair_out): half the butterflies of one FFT per line.
 __device__ __forceinline__ void dst_pair(double2* a, const double* x1, const double* x2, int64_t stride, int m, int lg,
-                                         const double2* __restrict__ tw) {
+                                         const double2* tw) {
   const int n = 2 * (m + 1), N = m + 1;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     double e1 = 0.0, e2 = 0.0;
@@ -1029,7 +1211,7 @@ __device__ __forceinline__ void dst_pair(double2* a, const double* x1, const dou
     for (int j = threadIdx.x; j < n / 2; j += blockDim.x) {
       const int pos = j & (half - 1);
       const int i0 = ((j >> (l - 1)) << l) + pos, i1 = i0 + half;
-      const double2 w = __ldg(tw + pos * tstride);
+      const double2 w = tw[pos * tstride];
       const double2 u = a[i0], v = a[i1];
       const double2 t = make_double2(fma(w.x, v.x, -w.y * v.y), fma(w.x, v.y, w.y * v.x));
       a[i0] = make_double2(u.x + t.x, u.y + t.y);
@@ -1039,19 +1221,27 @@ __device__ __forceinline__ void dst_pair(double2* a, const double* x1, const dou
   }
 }
 
+// the twiddles of a transform into shared memory (visible after the caller's next barrier)
+__device__ __forceinline__ void load_twiddles(double2* dst, const double2* __restrict__ src, int count) {
+  for (int i = threadIdx.x; i < count; i += blockDim.x) dst[i] = __ldg(src + i);
+}
+
 // the two lines' DST-I values at k = 1..m from the transformed buffer
 __device__ __forceinline__ double2 dst_pair_out(const double2* a, int n, int k) {
   const double2 zk = a[k], zn = a[n - k];
   return make_double2(-0.25 * (zk.y - zn.y), 0.25 * (zk.x - zn.x));
 }
 
-// rows: out(w, iy, k) = DST_x of rows iy = 2 blockIdx.x and 2 blockIdx.x + 1 of problem
-// w0 + blockIdx.y; `in_faces`: the input is a face vector (N x W, factor's face order) read
-// through grid_face, else a (W, my, mx) scratch; `out_faces` likewise for the output
-__global__ void k_dst_rows(DstArgs d, const double* in, double* out, int W, int w0, int in_faces, int out_faces) {
+// rows: out(w, iy, k) = DST_x of rows iy = lines blockIdx.x .. + lines - 1 (lines: 1 or 2) of
+// problem w0 + blockIdx.y; `in_faces`: the input is a face vector (N x W, factor's face order)
+// read through grid_face, else a (W, my, mx) scratch; `out_faces` likewise for the output
+__global__ void k_dst_rows(DstArgs d, const double* in, double* out, int W, int w0, int in_faces, int out_faces,
+                           int lines) {
   extern __shared__ double2 fft_buf[];
-  const int iy0 = 2 * blockIdx.x, iy1 = iy0 + 1, w = w0 + blockIdx.y, n = 2 * (d.mx + 1);
-  const bool two = iy1 < d.my;
+  const int iy0 = lines * blockIdx.x, iy1 = iy0 + 1, w = w0 + blockIdx.y, n = 2 * (d.mx + 1);
+  const bool two = lines == 2 && iy1 < d.my;
+  double2* tws = fft_buf + n + d.mx;   // after the FFT buffer and two lines (2 mx doubles)
+  load_twiddles(tws, d.twx, n / 2);
   const double *src0, *src1 = nullptr;
   if (in_faces) {
     // gather both rows through the face map after the FFT buffer
@@ -1067,7 +1257,7 @@ __global__ void k_dst_rows(DstArgs d, const double* in, double* out, int W, int 
     src0 = in + ((int64_t)w * d.my + iy0) * d.mx;
     if (two) src1 = src0 + d.mx;
   }
-  dst_pair(fft_buf, src0, src1, 1, d.mx, d.lgx, d.twx);
+  dst_pair(fft_buf, src0, src1, 1, d.mx, d.lgx, tws);
   for (int k = threadIdx.x; k < d.mx; k += blockDim.x) {
     const double2 y = dst_pair_out(fft_buf, n, k + 1);
     if (out_faces) {
@@ -1080,15 +1270,17 @@ __global__ void k_dst_rows(DstArgs d, const double* in, double* out, int W, int 
   }
 }
 
-// columns kx = 2 blockIdx.x and 2 blockIdx.x + 1: DST_y, division by the eigenvalues times the
+// columns kx = lines blockIdx.x .. + lines - 1: DST_y, division by the eigenvalues times the
 // scale, inverse DST_y (DST-I is its own inverse up to the scale)
-__global__ void k_dst_cols(DstArgs d, int w0) {
+__global__ void k_dst_cols(DstArgs d, int w0, int lines) {
   extern __shared__ double2 fft_buf[];
-  const int kx0 = 2 * blockIdx.x, kx1 = kx0 + 1, w = w0 + blockIdx.y, n = 2 * (d.my + 1);
-  const bool two = kx1 < d.mx;
+  const int kx0 = lines * blockIdx.x, kx1 = kx0 + 1, w = w0 + blockIdx.y, n = 2 * (d.my + 1);
+  const bool two = lines == 2 && kx1 < d.mx;
   const double* col = d.t1 + (int64_t)w * d.my * d.mx + kx0;
   double* tmp = reinterpret_cast<double*>(fft_buf + n);   // 2 x my values after the FFT buffer
-  dst_pair(fft_buf, col, two ? col + 1 : nullptr, d.mx, d.my, d.lgy, d.twy);
+  double2* tws = fft_buf + n + d.my;                      // then the twiddles
+  load_twiddles(tws, d.twy, n / 2);
+  dst_pair(fft_buf, col, two ? col + 1 : nullptr, d.mx, d.my, d.lgy, tws);
   const double lx0 = __ldg(d.lamx + kx0), lx1 = two ? __ldg(d.lamx + kx1) : 0.0;
   for (int k = threadIdx.x; k < d.my; k += blockDim.x) {
     const double2 y = dst_pair_out(fft_buf, n, k + 1);
@@ -1097,7 +1289,7 @@ __global__ void k_dst_cols(DstArgs d, int w0) {
     tmp[d.my + k] = two ? y.y * d.scale / (lx1 + ly) : 0.0;
   }
   __syncthreads();
-  dst_pair(fft_buf, tmp, two ? tmp + d.my : nullptr, 1, d.my, d.lgy, d.twy);
+  dst_pair(fft_buf, tmp, two ? tmp + d.my : nullptr, 1, d.my, d.lgy, tws);
   double* out = d.t2 + (int64_t)w * d.my * d.mx + kx0;
   for (int k = threadIdx.x; k < d.my; k += blockDim.x) {
     const double2 y = dst_pair_out(fft_buf, n, k + 1);
@@ -1277,6 +1469,13 @@ struct Schedule {
   std::vector<int32_t> pack_sn;
   std::vector<int4> pack_meta;
   std::vector<double> pack_vals;
+  // subtree sweeps (k_subtree): the subtrees, per supernode metadata (members only), the local
+  // row maps, the largest subtree's sizes; their members have no level items
+  std::vector<SubTree> subs;
+  std::vector<int4> sub_meta;
+  std::vector<int32_t> sub_lrow;
+  std::vector<uint16_t> sub_loc;
+  int sub_max_rows = 0, sub_max_f = 0, sub_max_n = 0, sub_max_l = 0;
 };
 
 // the supernodes a work item covers: one, or the members of a W = 1 pack
@@ -1291,6 +1490,94 @@ void for_each_supernode(const Schedule& S, const int4& v, Fn fn) {
   for (int l = 0; l < v.y; ++l) fn(S.pack_sn[first + l]);
 }
 
+// Subtrees for k_subtree: the largest subtrees whose columns plus their root's off-diagonal rows
+// number at most `max_rows`, with no member wider than kSubMaxK columns and bounded staging (F
+// values, local row maps). Every limit grows towards the root, so a qualifying supernode's
+// descendants qualify and the subtrees are the qualifying supernodes whose parent does not.
+// Marks the members in `inside`, re-levels the others in `level` (leaves 0, all subtrees below
+// level 0) and sets S.n_levels.
+void build_subtrees(const jja::Factor& F, int max_rows, Schedule& S, std::vector<char>& inside,
+                    std::vector<int>& level) {
+  const int ns = F.ns;
+  std::vector<int64_t> cols(ns), fl(ns), ll(ns);
+  std::vector<int> kmax(ns), cnt(ns);
+  for (int s = 0; s < ns; ++s) {
+    const int k = F.sn_k[s], m = F.sn_m[s];
+    cols[s] = k;
+    fl[s] = (int64_t)(k + m) * k;
+    ll[s] = m;
+    kmax[s] = k;
+    cnt[s] = 1;
+  }
+  for (int s = 0; s < ns; ++s) {
+    const int p = F.sn_parent[s];
+    if (p < 0) continue;
+    if (p <= s || p >= ns) throw Error(JJA_ERR_INTERNAL, "supernodes are not in postorder");
+    cols[p] += cols[s];
+    fl[p] += fl[s];
+    ll[p] += ll[s];
+    kmax[p] = std::max(kmax[p], kmax[s]);
+    cnt[p] += cnt[s];
+  }
+  std::vector<char> ok(ns);
+  for (int s = 0; s < ns; ++s)
+    ok[s] = cols[s] + F.sn_m[s] <= max_rows && kmax[s] <= kSubMaxK && fl[s] <= kSubMaxF && ll[s] <= kSubMaxL;
+  S.sub_meta.assign(ns, make_int4(0, 0, 0, 0));
+  S.sub_lrow.assign(ns, 0);
+  for (int t = 0; t < ns; ++t) {
+    const int p = F.sn_parent[t];
+    if (!ok[t] || (p >= 0 && ok[p])) continue;
+    SubTree T{};
+    T.n = cnt[t];
+    T.s0 = t - cnt[t] + 1;
+    T.c0 = F.sn_col0[T.s0];
+    T.ncols = (int)cols[t];
+    T.m_root = F.sn_m[t];
+    if (T.c0 + T.ncols != F.sn_col0[t] + F.sn_k[t]) throw Error(JJA_ERR_INTERNAL, "subtree columns are not contiguous");
+    T.f_off = F.sn_valptr[T.s0];
+    T.f_len = (int)(F.sn_valptr[t + 1] - T.f_off);
+    T.r_off = F.sn_rowptr[t];
+    T.l_off = (int64_t)S.sub_loc.size();
+    T.l_len = (int)(F.sn_rowptr[t + 1] - F.sn_rowptr[T.s0]);
+    const int c_end = T.c0 + T.ncols;
+    const int* Rr = F.rows.data() + F.sn_rowptr[t];
+    for (int u = T.s0; u <= t; ++u) {
+      if (!ok[u] || inside[u]) throw Error(JJA_ERR_INTERNAL, "subtree member does not qualify");
+      inside[u] = 1;
+      const int k = F.sn_k[u];
+      S.sub_meta[u] = make_int4(F.sn_col0[u] - T.c0, k, k + F.sn_m[u], (int)(F.sn_valptr[u] - T.f_off));
+      S.sub_lrow[u] = (int32_t)(F.sn_rowptr[u] - F.sn_rowptr[T.s0]);
+      for (int64_t q = F.sn_rowptr[u]; q < F.sn_rowptr[u + 1]; ++q) {
+        const int r = F.rows[q];
+        int local;
+        if (r >= T.c0 && r < c_end) {
+          local = r - T.c0;
+        } else {
+          const int* hit = std::lower_bound(Rr, Rr + T.m_root, r);
+          if (hit == Rr + T.m_root || *hit != r) throw Error(JJA_ERR_INTERNAL, "subtree row outside its root's structure");
+          local = T.ncols + (int)(hit - Rr);
+        }
+        S.sub_loc.push_back((uint16_t)local);
+      }
+    }
+    S.sub_max_rows = std::max(S.sub_max_rows, T.ncols + T.m_root);
+    S.sub_max_f = std::max(S.sub_max_f, (T.f_len + 1) / 2 * 2);
+    S.sub_max_n = std::max(S.sub_max_n, T.n);
+    S.sub_max_l = std::max(S.sub_max_l, T.l_len);
+    S.subs.push_back(T);
+  }
+  // the remaining supernodes: leaves (or parents of subtrees only) at level 0
+  int top = -1;
+  for (int s = 0; s < ns; ++s) if (!inside[s]) level[s] = 0;
+  for (int s = 0; s < ns; ++s) {
+    if (inside[s]) continue;
+    top = std::max(top, level[s]);
+    const int p = F.sn_parent[s];
+    if (p >= 0) level[p] = std::max(level[p], level[s] + 1);
+  }
+  S.n_levels = top + 1;
+}
+
 // the work items of problems [w_lo, w_hi) (w_hi < 0: all W); w_lo a multiple of the RHS block
 Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu, int w_lo = 0, int w_hi = -1) {
   if (W <= 0 || W >= (1 << 30)) throw Error(JJA_ERR_ARG, "W must be in [1, 2^30)");
@@ -1300,6 +1587,8 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
   if (tu.target_warps < 0 || tu.min_piece < 0) throw Error(JJA_ERR_ARG, "target_warps and min_piece must be >= 0");
   if (tu.schedule < 0 || tu.schedule > 3) throw Error(JJA_ERR_ARG, "schedule must be 0, 1, 2 or 3");
   if (tu.coop_blocks < 0) throw Error(JJA_ERR_ARG, "coop_blocks must be >= 0");
+  if (tu.dst_lines < 0 || tu.dst_lines > 2) throw Error(JJA_ERR_ARG, "dst_lines must be 0, 1 or 2");
+  if (tu.subtree_rows > 64) throw Error(JJA_ERR_ARG, "subtree_rows must be <= 64");
   if (tu.pdl < 0 || tu.pdl > 1) throw Error(JJA_ERR_ARG, "pdl must be 0 or 1");
   if (tu.pack_rows > 256) throw Error(JJA_ERR_ARG, "pack_rows must be <= 256");
   if (tu.pack_min_warps < 0) throw Error(JJA_ERR_ARG, "pack_min_warps must be >= 0");
@@ -1319,12 +1608,20 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
   Schedule S;
   S.n_levels = F.n_levels;
   S.ns = F.ns;
-  std::vector<std::vector<int>> by_level(F.n_levels);
   for (int s = 0; s < F.ns; ++s) {
     if (F.sn_level[s] < 0 || F.sn_level[s] >= F.n_levels) throw Error(JJA_ERR_INTERNAL, "supernode level out of range");
-    by_level[F.sn_level[s]].push_back(s);
     if (F.sn_k[s] + F.sn_m[s] >= 65536) throw Error(JJA_ERR_ARG, "supernode with >= 65536 rows");
   }
+  // subtree sweeps at the bottom of the tree (level schedule, 32 problems per warp); the other
+  // supernodes are re-levelled above them
+  const int sub_rows = (WB == 32 && tu.schedule <= 1 && tu.subtree_rows >= 0)
+                           ? (tu.subtree_rows ? tu.subtree_rows : kDefaultSubRows) : 0;
+  std::vector<int> level(F.sn_level.begin(), F.sn_level.end());
+  std::vector<char> inside(F.ns, 0);
+  if (sub_rows > 0) build_subtrees(F, sub_rows, S, inside, level);
+  std::vector<std::vector<int>> by_level(S.n_levels);
+  for (int s = 0; s < F.ns; ++s)
+    if (!inside[s]) by_level[level[s]].push_back(s);
   auto pack = [](int s, int r0, int r1, int w0, bool partial, int c_lo, int c_hi) {
     return make_int4(s, r0 | (r1 << 16), w0 | ((int)partial << 30), c_lo | (c_hi << 16));
   };
@@ -1338,7 +1635,7 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
   };
   S.fwd_ptr.assign(1, 0);
   S.bwd_ptr.assign(1, 0);
-  for (int l = 0; l < F.n_levels; ++l) {
+  for (int l = 0; l < S.n_levels; ++l) {
     int64_t nfw = 0, nbw = 0;
     for (int s : by_level[l]) {
       const int k = F.sn_k[s], nf = k + F.sn_m[s];
@@ -1414,7 +1711,7 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
     S.fwd_ptr.push_back((int64_t)S.fi.size());
     S.bwd_ptr.push_back((int64_t)S.bi.size());
   }
-  for (int l = F.n_levels - 1; l >= 0; --l)
+  for (int l = S.n_levels - 1; l >= 0; --l)
     S.bi_flow.insert(S.bi_flow.end(), S.bi.begin() + S.bwd_ptr[l], S.bi.begin() + S.bwd_ptr[l + 1]);
   const int ns = F.ns;
   std::vector<uint32_t> nfi(ns, 0), nbi(ns, 0);
@@ -1616,7 +1913,9 @@ struct jja_plan {
   unsigned* coop_bar = nullptr;
   bool coop_packs = false;
   // fast Poisson solve of uniform square arrays (jja_plan_set_fast_poisson): replaces both sweeps
+  SubDev sub{};        // subtree sweeps (k_subtree; n = 0: none)
   int dst = 0;
+  int dst_lines = 0;   // grid lines per block of the sine-transform kernels (0: by grid size)
   DstArgs dst_args{};
   std::vector<int32_t> iperm_host;   // original face -> factor's face order
   int64_t bytes = 0;
@@ -1660,6 +1959,28 @@ void launch(bool pdl, void (*kernel)(KArgs...), int grid, int block, cudaStream_
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3((unsigned)block);
     cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    JJA_CUDA(cudaLaunchKernelEx(&cfg, kernel, args...));
+  }
+  g_launches++;
+}
+
+// the same with a 2-D grid and dynamic shared memory
+template <typename... KArgs, typename... Args>
+void launch_smem(bool pdl, void (*kernel)(KArgs...), dim3 grid, int block, size_t smem, cudaStream_t st,
+                 Args... args) {
+  if (!pdl) {
+    kernel<<<grid, block, smem, st>>>(args...);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -1751,6 +2072,17 @@ void launch_coop(jja_plan* p, cudaStream_t st, bool forward, double* b, double* 
   g_launches++;
 }
 
+// the subtree sweep of group g (before the forward levels, after the backward ones)
+void launch_subtrees(jja_plan* p, const Group& g, cudaStream_t st, bool forward, double* b, double* z, double* x) {
+  if (!p->sub.n) return;
+  const int blocks = (g.wn + 31) / 32;
+  const int warps = std::min(blocks, kSubMaxWarps);
+  const dim3 grid((unsigned)p->sub.n, (unsigned)((blocks + warps - 1) / warps));
+  const size_t smem = sub_smem_bytes(p->sub, warps);
+  launch_smem(p->pdl, forward ? k_subtree<true> : k_subtree<false>, grid, warps * 32, smem, st, p->F, p->sub, p->W,
+              g.w0, g.wn, b, z, x);
+}
+
 template <int RPL>
 void launch_sweep(jja_plan* p, const Group& g, cudaStream_t st, bool forward, double* b, double* z, double* x) {
   if (p->flow) {
@@ -1762,6 +2094,7 @@ void launch_sweep(jja_plan* p, const Group& g, cudaStream_t st, bool forward, do
     return;
   }
   if (forward) {  // levels ascending (children before parents); b is consumed, z produced
+    launch_subtrees(p, g, st, true, b, z, x);
     for (int l = 0; l < p->n_levels; ++l) {
       const int n = (int)(g.fwd_ptr[l + 1] - g.fwd_ptr[l]);
       if (!n) continue;
@@ -1777,6 +2110,7 @@ void launch_sweep(jja_plan* p, const Group& g, cudaStream_t st, bool forward, do
              (n + kWarpsPerBlock - 1) / kWarpsPerBlock, kWarpsPerBlock * 32, st, p->F,
              (const int4*)(g.bwd_items + g.bwd_ptr[l]), n, p->W, p->WB, (const double*)z, x);
     }
+    launch_subtrees(p, g, st, false, b, z, x);
   }
 }
 
@@ -1799,7 +2133,6 @@ void launch_levels(jja_plan* p, const Group& g, cudaStream_t st, bool forward) {
   launch_sweep_any(p, g, st, forward, p->b, p->z, p->x);
 }
 
-void launch_levels(jja_plan* p, cudaStream_t st, bool forward) { launch_levels(p, p->all, st, forward); }
 
 // x = K^-1 b for group g: the two triangular sweeps, or the three sine-transform kernels
 void launch_face_solve(jja_plan* p, const Group& g, cudaStream_t st) {
@@ -1809,14 +2142,18 @@ void launch_face_solve(jja_plan* p, const Group& g, cudaStream_t st) {
     return;
   }
   const DstArgs& d = p->dst_args;
-  // an FFT buffer of 2 (m + 1) complex points, then two lines of m values
-  const size_t smx = (size_t)2 * (d.mx + 1) * sizeof(double2) + (size_t)2 * d.mx * sizeof(double);
-  const size_t smy = (size_t)2 * (d.my + 1) * sizeof(double2) + (size_t)2 * d.my * sizeof(double);
+  // an FFT buffer of 2 (m + 1) complex points, two lines of m values, m + 1 twiddles
+  const size_t smx = (size_t)3 * (d.mx + 1) * sizeof(double2) + (size_t)2 * d.mx * sizeof(double);
+  const size_t smy = (size_t)3 * (d.my + 1) * sizeof(double2) + (size_t)2 * d.my * sizeof(double);
   const int tx = std::min(512, d.mx + 1), ty = std::min(512, d.my + 1);
-  const unsigned row_pairs = (unsigned)((d.my + 1) / 2), col_pairs = (unsigned)((d.mx + 1) / 2);
-  k_dst_rows<<<dim3(row_pairs, (unsigned)g.wn), tx, smx, st>>>(d, p->b, d.t1, p->W, g.w0, 1, 0);
-  k_dst_cols<<<dim3(col_pairs, (unsigned)g.wn), ty, smy, st>>>(d, g.w0);
-  k_dst_rows<<<dim3(row_pairs, (unsigned)g.wn), tx, smx, st>>>(d, d.t2, p->x, p->W, g.w0, 0, 1);
+  // two lines per block halve the butterflies but also the blocks: pair only while the
+  // smaller grid still fills every SM twice
+  const int lines = p->dst_lines ? p->dst_lines
+                                 : ((int64_t)((std::min(d.mx, d.my) + 1) / 2) * g.wn >= 2 * kNumSMs ? 2 : 1);
+  const unsigned row_blocks = (unsigned)((d.my + lines - 1) / lines), col_blocks = (unsigned)((d.mx + lines - 1) / lines);
+  k_dst_rows<<<dim3(row_blocks, (unsigned)g.wn), tx, smx, st>>>(d, p->b, d.t1, p->W, g.w0, 1, 0, lines);
+  k_dst_cols<<<dim3(col_blocks, (unsigned)g.wn), ty, smy, st>>>(d, g.w0, lines);
+  k_dst_rows<<<dim3(row_blocks, (unsigned)g.wn), tx, smx, st>>>(d, d.t2, p->x, p->W, g.w0, 0, 1, lines);
   g_launches += 3;
 }
 
@@ -2085,6 +2422,7 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     p->rows_per_lane = rows_per_lane_of(tu, false, d->W);
     p->rows_per_lane_fwd = rows_per_lane_of(tu, true, d->W);
     p->pdl = tu.pdl == 1;
+    p->dst_lines = tu.dst_lines;
     const int Nj = d->Nj, Nf = d->Nf;
     const FaceTables ft = face_tables(Nj, Nf, d->a_rowptr, d->a_col, d->a_val, F.perm);
     {
@@ -2163,6 +2501,22 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
       JJA_CUDA(cudaMemset(g.d_step, 0, 4 * sizeof(int64_t)));
     };
     set_group(p->all, S, 0, d->W);
+    if (!S.subs.empty()) {
+      SubDev& sd = p->sub;
+      sd.tab = p->up(S.subs.data(), S.subs.size());
+      sd.meta = p->up(S.sub_meta.data(), S.sub_meta.size());
+      sd.lrow = p->up(S.sub_lrow.data(), S.sub_lrow.size());
+      sd.loc = p->up(S.sub_loc.data(), S.sub_loc.size());
+      sd.n = (int)S.subs.size();
+      sd.max_rows = S.sub_max_rows;
+      sd.max_f = S.sub_max_f;
+      sd.max_n = S.sub_max_n;
+      sd.max_l = S.sub_max_l;
+      const size_t smem = sub_smem_bytes(sd, kSubMaxWarps);
+      if (smem > (size_t)227 * 1024) throw Error(JJA_ERR_INTERNAL, "subtree staging exceeds shared memory");
+      JJA_CUDA(cudaFuncSetAttribute(k_subtree<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      JJA_CUDA(cudaFuncSetAttribute(k_subtree<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
     p->bwd_flow_items = p->up(S.bi_flow.data(), S.bi_flow.size());
     p->F.pack_meta = p->up(S.pack_meta.data(), S.pack_meta.size());
     p->F.pack_vals = p->up(S.pack_vals.data(), S.pack_vals.size());
@@ -2180,7 +2534,10 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
         for (int gi = 0; gi < ng; ++gi) {
           const int lo = (int)((int64_t)chunks * gi / ng) * p->WB;
           const int hi = std::min(d->W, (int)((int64_t)chunks * (gi + 1) / ng) * p->WB);
-          set_group(p->groups[gi], build_schedule(F, d->W, tu, lo, hi), lo, hi - lo);
+          const Schedule Sg = build_schedule(F, d->W, tu, lo, hi);
+          if (Sg.n_levels != S.n_levels || Sg.subs.size() != S.subs.size())
+            throw Error(JJA_ERR_INTERNAL, "group schedules differ in levels or subtrees");
+          set_group(p->groups[gi], Sg, lo, hi - lo);
           if (gi > 0) JJA_CUDA(cudaStreamCreateWithFlags(&p->groups[gi].stream, cudaStreamNonBlocking));
           JJA_CUDA(cudaEventCreateWithFlags(&p->groups[gi].done, cudaEventDisableTiming));
         }
@@ -2307,6 +2664,9 @@ int jja_plan_set_fast_poisson(jja_plan* p, int mx, int my, const int32_t* grid_f
     d.scale = (double)((4.0L / ((long double)(mx + 1) * (my + 1))) / kappa);
     d.t1 = p->up<double>(nullptr, (size_t)p->Nf * p->W);
     d.t2 = p->up<double>(nullptr, (size_t)p->Nf * p->W);
+    const int smem_max = (int)(3 * 1024 * sizeof(double2) + 2 * 1023 * sizeof(double));
+    JJA_CUDA(cudaFuncSetAttribute(k_dst_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+    JJA_CUDA(cudaFuncSetAttribute(k_dst_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
     // graphs captured before bake in the sweeps: drop them
     for (auto& g : p->graphs) cudaGraphExecDestroy(g.exec);
     for (auto& g : p->adj_graphs) cudaGraphExecDestroy(g.exec);

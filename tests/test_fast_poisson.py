@@ -50,6 +50,18 @@ def test_fast_poisson_solve_matches_scipy(nx, ny, W):
     assert float(np.abs(x - ref).max()) <= 1e-11 * float(np.abs(ref).max())
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("lines", [1, 2])
+@pytest.mark.parametrize("nx,ny,W", [(64, 32, 3), (256, 256, 1)])
+def test_one_and_two_lines_per_block_agree(nx, ny, W, lines):
+    c = SquareArray(nx, ny)
+    A, K = P.face_matrix(c, 0.05)
+    b = np.random.default_rng(5).standard_normal((K.shape[0], W))
+    x = backend.solve_faces(c, 0.05, b, fast_poisson=True, tuning={"dst_lines": lines})
+    ref = scipy.sparse.linalg.spsolve(K.tocsc(), b).reshape(x.shape)
+    assert float(np.abs(x - ref).max()) <= 1e-11 * float(np.abs(ref).max())
+
+
 def _problem(c, W, Nt):
     Is = c.current_base(0.0)[:, None, None] * np.linspace(0.4, 1.6, W)[None, :, None]
     return TimeEvolutionProblem(c, time_step=0.05, time_step_count=Nt, current_sources=Is, external_flux=0.13,

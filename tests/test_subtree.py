@@ -1,0 +1,74 @@
+"""Subtree sweeps: the bottom of the elimination tree solved one warp per (subtree, 32 problems)
+in shared memory (k_subtree), before the forward levels and after the backward ones.
+
+CPU: the schedule with subtrees builds and passes its dataflow check on several lattices and
+orderings; subtrees take the place of most bottom-level items; the size bound is validated.
+GPU: face solves against scipy's sparse direct solve (relative 1e-11) with subtrees of several
+sizes, partial warps (W not a multiple of 32) and concurrent problem groups; trajectories with
+and without subtrees agree to 1e-11 relative (only the summation order differs).
+"""
+import numpy as np
+import pytest
+import scipy.sparse.linalg
+
+from pyjjasim_gb300 import TimeEvolutionProblem, backend
+from pyjjasim_gb300 import _native as N
+from pyjjasim_gb300 import plan as P
+from pyjjasim_gb300.circuit import HoneycombArray, SquareArray, TriangularArray
+
+LATTICES = {"square": SquareArray, "honeycomb": HoneycombArray, "triangular": TriangularArray}
+
+
+def _factor(c, W, ordering):
+    return P.get_factor(c, 0.05, nd_leaf=8, ordering=ordering)[0]
+
+
+@pytest.mark.parametrize("lattice,n,ordering", [("square", 64, "nd"), ("square", 96, "mmd"),
+                                                ("honeycomb", 40, "nd"), ("triangular", 48, "mmd")])
+def test_schedule_with_subtrees(lattice, n, ordering):
+    f = _factor(LATTICES[lattice](n, n), 64, ordering)
+    n_off = f.check_schedule(64, {"subtree_rows": -1})
+    for rows in (0, 8, 32, 64):
+        n_on = f.check_schedule(64, {"subtree_rows": rows})
+        assert n_on[0] < n_off[0] and n_on[1] <= n_off[1]
+    # below 32 problems per warp no subtrees are built
+    assert f.check_schedule(8, {}) == f.check_schedule(8, {"subtree_rows": -1})
+
+
+def test_subtree_rows_bound():
+    f = _factor(SquareArray(16, 16), 32, "nd")
+    with pytest.raises(N.JJAError):
+        f.check_schedule(32, {"subtree_rows": 65})
+
+
+def _rhs(K, W, seed):
+    return np.random.default_rng(seed).standard_normal((K.shape[0], W))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lattice,n,W,ordering", [("square", 128, 512, "mmd"), ("square", 64, 48, "nd"),
+                                                  ("honeycomb", 40, 32, "nd"), ("triangular", 48, 96, "mmd")])
+@pytest.mark.parametrize("rows", [0, 8, 64])
+def test_subtree_solve_matches_scipy(lattice, n, W, ordering, rows):
+    c = LATTICES[lattice](n, n)
+    c.set_inductance(0.03)
+    A, K = P.face_matrix(c, 0.05)
+    b = _rhs(K, W, n + W + rows)
+    x = backend.solve_faces(c, 0.05, b, ordering=ordering, tuning={"subtree_rows": rows})
+    ref = scipy.sparse.linalg.spsolve(K.tocsc(), b).reshape(x.shape)
+    assert float(np.abs(x - ref).max()) <= 1e-11 * float(np.abs(ref).max())
+
+
+@pytest.mark.gpu
+def test_trajectories_with_and_without_subtrees_agree():
+    c = SquareArray(48, 48)
+    c.set_capacitance(0.3)
+    W, Nt = 288, 150           # two problem groups; the last warp of each group partly idle
+    Is = c.current_base(0.0)[:, None, None] * np.linspace(0.2, 1.8, W)[None, :, None]
+    prob = TimeEvolutionProblem(c, time_step=0.05, time_step_count=Nt, current_sources=Is, external_flux=0.2,
+                                store_time_steps=[Nt // 2, Nt - 1])
+    mask = prob.store_time_steps
+    th_on, _ = backend.time_evolution_core(prob, mask, mask, tuning={"subtree_rows": 32})
+    th_off, _ = backend.time_evolution_core(prob, mask, mask, tuning={"subtree_rows": -1})
+    scale = max(1.0, float(np.abs(th_off).max()))
+    assert float(np.abs(th_on - th_off).max()) <= 1e-11 * scale
