@@ -628,6 +628,22 @@ def profile_mode(args):
         ok = bool(sim.plan.fast_poisson) and bool(torch.isfinite(sim.theta()).all())
         print(json.dumps({"profile_case": "fast_poisson", "steps": 3 + args.profile_steps, "ok": ok}))
         sys.exit(0 if ok else 1)
+    if args.profile_case == "ragged":
+        # the W = 1 level kernels on a block-diagonal union: the first 8 problems of the ragged
+        # draws as one part (sources zero: the kernels' cost does not depend on the values)
+        from pyjjasim_gb300.ragged import RaggedBatch
+        kinds, sizes = ragged_draws()
+        lattices = (G.SquareArray, G.HoneycombArray, G.TriangularArray)
+        probs = [G.TimeEvolutionProblem(lattices[k](int(nn), int(nn)), time_step=0.05, time_step_count=10 ** 6,
+                                        external_flux=0.25)
+                 for k, nn in list(zip(kinds, sizes))[:8]]
+        sim = RaggedBatch(probs, parts=1).simulations()[0]
+        sim.run(3 + args.profile_steps, use_graph=False)
+        sim.synchronize()
+        ok = bool(torch.isfinite(sim.theta()).all())
+        print(json.dumps({"profile_case": "ragged", "problems": 8, "junctions": sim.plan.Nj,
+                          "steps": 3 + args.profile_steps, "ok": ok}))
+        sys.exit(0 if ok else 1)
     if args.profile_case == "static":
         # the static solver's refactorisation: 64 problems on SquareArray(64,64), L = 0.1
         from pyjjasim_gb300.static import StaticProblem, compute_many
@@ -661,8 +677,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--profile-case", default="iv", choices=["iv", "fast_poisson", "static"],
-                    help="profiling mode: the IV sweep (default), the fast Poisson single array, the static solver")
+    ap.add_argument("--profile-case", default="iv", choices=["iv", "fast_poisson", "static", "ragged"],
+                    help="profiling mode: the IV sweep (default), the fast Poisson single array, the static "
+                         "solver, the W = 1 ragged union")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling mode: plan, 3 eager warm-up steps, then this many eager steps, nothing else")
     ap.add_argument("--W", type=int, default=W_BATCH, help="problems per launch (profiling mode)")

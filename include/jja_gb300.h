@@ -96,7 +96,7 @@ typedef struct {
                          columns) are solved one per lane, 32 per warp (0: default 24; negative:
                          never) ... */
   int pack_min_warps; /* ... on levels whose regular items need at least this many warps
-                         (0: default 19456, two waves of 152 SMs x 64 warps) */
+                         (0: default 4864, half a wave of 152 SMs x 64 warps) */
   int pdl;            /* 1: launch the step's kernels with programmatic dependent launch (each
                          launch overlaps the tail of the kernel before; measured: 6 % faster for
                          W = 1, 5-7 % slower for W >= 64); 0: default (plain launches) */
@@ -109,11 +109,16 @@ typedef struct {
   int dst_lines;      /* fast Poisson solve (jja_plan_set_fast_poisson): grid lines per block of the
                          sine-transform kernels, 1 or 2 (two real lines share one complex FFT);
                          0: default (2 when that still gives at least 2 x 152 blocks, else 1) */
+  int pack_lanes;     /* W = 1 packs: lanes per packed supernode, 1, 2 or 4 (its rows split between
+                         them; 32 / pack_lanes supernodes per warp); 0: default (per level: 4 where
+                         one lane per supernode would give fewer than 4096 warps, else 1) */
   int subtree_rows;   /* level schedule with 32 problems per warp (W >= 17): subtrees at the bottom of
                          the elimination tree spanning at most this many rows (their columns plus
                          their root's off-diagonal rows, <= 64) are solved one warp per subtree and
                          32 problems in shared memory, one launch per sweep, before the levels
-                         above them; 0: default (32); negative: never */
+                         above them; 0: default (32 rows, where the subtree launch has at least
+                         152 x 16 warps: measured 5-8 % faster per step at W = 512-1024 on 128x128
+                         arrays, 7 % slower at W = 64 on 64x64 with 500 warps); negative: never */
 } jja_solve_tuning;
 
 /* Builds on the host (no GPU needed) the work-item schedule that jja_plan_create would make for

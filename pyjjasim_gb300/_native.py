@@ -32,7 +32,8 @@ class SolveTuning(ctypes.Structure):
     _fields_ = [("rhs_block", c_int), ("rows_per_lane", c_int), ("target_warps", c_int), ("min_piece", c_int),
                 ("schedule", c_int), ("rows_per_lane_fwd", c_int), ("pack_rows", c_int), ("pack_min_warps", c_int),
                 ("pdl", c_int), ("groups", c_int), ("coop_blocks", c_int),
-                ("dst_lines", c_int), ("subtree_rows", c_int)]
+                ("dst_lines", c_int), ("pack_lanes", c_int),
+                ("subtree_rows", c_int)]
 
 
 class PlanDesc(ctypes.Structure):

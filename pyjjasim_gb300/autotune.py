@@ -20,7 +20,9 @@ GPU depends on choices that have no single best value across array sizes and bat
 * ``rhs_block`` (a power of two <= 32): problems a warp handles side by side (the remaining
   lanes take more rows);
 * ``target_warps``: how aggressively the few, long dot products at the top of the elimination
-  tree are split into atomically accumulated pieces.
+  tree are split into atomically accumulated pieces;
+* ``subtree_rows``: from 32 problems per warp, how large the subtrees at the bottom of the tree
+  are that one warp solves in shared memory (0: the library's rule; -1: none).
 
 ``autotune`` times candidates with CUDA events on graph-replayed steps of a synthetic problem
 on the same circuit, time step, stencil width and W (the step's cost does not depend on the
@@ -39,13 +41,13 @@ from . import plan as P
 
 CACHE_ENV = "PYJJASIM_GB300_TUNE_CACHE"
 DEFAULT = {"schedule": 1, "ordering": "auto", "relax": (-1, -1.0), "rows_per_lane": 0, "rows_per_lane_fwd": 0,
-           "rhs_block": 0, "target_warps": 152 * 24, "pdl": 0, "groups": 0}
+           "rhs_block": 0, "target_warps": 152 * 24, "pdl": 0, "groups": 0, "subtree_rows": 0}
 # searched in this order; a tuple is searched jointly (ordering and rows per lane interact:
 # minimum degree's smaller supernodes want fewer rows per warp). Rows per lane 0 = the library's
 # defaults (1, and 2 in the forward sweep from W = 256 on); a nonzero value sets both sweeps
 # unless rows_per_lane_fwd sets the forward one.
 AXES = (("ordering", "rows_per_lane"), "rows_per_lane_fwd", "schedule", "pdl", "groups", "rhs_block", "target_warps",
-        "relax")
+        "subtree_rows", "relax")
 
 
 def cache_path():
@@ -72,6 +74,7 @@ def candidates(W):
         "rows_per_lane_fwd": [0, 1, 2, 4],
         "rhs_block": [0] + [b for b in (wb // 2, wb // 4) if b >= 1],
         "target_warps": [152 * 24, 152 * 8, 152 * 64],
+        "subtree_rows": [0, -1, 24, 48] if W >= 17 else [0],
         "relax": [(-1, -1.0), (0, 0.0), (64, 0.1)],
     }
 
@@ -83,7 +86,7 @@ def to_options(cfg):
                        "rows_per_lane_fwd": int(cfg.get("rows_per_lane_fwd", 0)),
                        "rhs_block": int(cfg["rhs_block"]), "target_warps": int(cfg["target_warps"]),
                        "schedule": int(cfg["schedule"]), "pdl": int(cfg.get("pdl", 0)),
-                       "groups": int(cfg.get("groups", 0))}}
+                       "groups": int(cfg.get("groups", 0)), "subtree_rows": int(cfg.get("subtree_rows", 0))}}
 
 
 def coordinate_descent(W, measure, min_gain=0.02):

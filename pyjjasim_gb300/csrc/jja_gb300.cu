@@ -73,13 +73,15 @@ constexpr int kDefaultRowsPerLane = 1;
 constexpr int kDefaultRowsPerLaneFwdWide = 2;   // the forward sweep's default for W >= 256
 constexpr int kDefaultPackRows = 24;   // W = 1: supernodes of at most this many rows go one per lane
 constexpr int kPackMaxK = 8;           // ... and at most this many columns
-constexpr int kDefaultPackMinWarps = 152 * 64 * 2;   // ... on levels with at least two waves of warps
+constexpr int kPackLanesWarps = 4096;  // ... 4 lanes each on levels with fewer one-lane pack warps
+constexpr int kDefaultPackMinWarps = 152 * 32;   // ... on levels whose regular items need this many warps
 constexpr int kGroupsFromW = 256;      // from this many problems the step runs as concurrent groups ...
 constexpr int kGroupW = 160;           // ... of about this many problems, 2 to 4 of them
 constexpr int kNumSMs = 152;                     // GB300
 constexpr int kDefaultTargetWarps = 152 * 24;   // levels with fewer work items split their dot products
 constexpr int kDefaultMinPiece = 16;     // shortest piece of a split dot product
 constexpr int kDefaultSubRows = 32;     // subtree sweeps: rows per subtree (columns + the root's off-diagonal rows)
+constexpr int kSubMinWarps = 152 * 16;  // ... by default only when the launch has at least this many warps
 constexpr int kSubMaxWarps = 8;         // ... warps (32-problem blocks of one subtree) per block
 constexpr int kSubMaxK = 8;             // ... members of at most this many columns
 constexpr int kSubMaxF = 2048;          // ... at most this many F values per subtree
@@ -598,19 +600,37 @@ struct FactorDev {
   const double* pack_vals;   // W = 1 packs: the F_s of a pack's supernodes interleaved by lane
 };
 
-// W = 1 packs. A work item whose x field is negative covers up to 32 small supernodes of one
-// level, one per lane: pack p = -1 - x, y lanes, z = NP | KP << 16 (the largest row and column
-// count among them), w = offset of its values in units of 32 doubles. F_s(r, j) of lane l sits at
-// pack_vals[32 (w + j NP + r) + l], zero padded to NP x KP, so every load instruction of the warp
-// reads 256 contiguous bytes while each lane walks its own supernode. Levels with many more
-// small supernodes than a wave of warps use them: a regular item there leaves most lanes idle and
-// pays a chain of dependent loads for a handful of FMAs. KM (>= KP) sizes the register arrays.
+// W = 1 packs. A work item whose x field is negative covers up to 32 / LPS small supernodes of
+// one level, LPS (1, 2 or 4) lanes each: pack p = -1 - x, y supernodes, z = NP | KP << 16 |
+// LPS << 24 (the largest row and column count among them), w = offset of its values in units
+// of 32 doubles. Lane l serves slot l / LPS (its supernode) and that supernode's rows
+// r = g + LPS rr, g = l % LPS; F_s(r, j) sits at pack_vals[32 (w + j NPq + rr) + l] with
+// NPq = ceil(NP / LPS), zero padded, so every load instruction of the warp reads 256
+// contiguous bytes while each lane walks its rows. Levels with many more small supernodes than
+// a wave of warps use them: a regular item there leaves most lanes idle and pays a chain of
+// dependent loads for a handful of FMAs; more lanes per supernode give more warps and shorter
+// chains per lane. KM (>= KP) sizes the register arrays.
+struct PackShape {
+  int count, NP, KP, LPS, NPq;
+};
+
+__device__ __forceinline__ PackShape pack_shape(const int4 raw) {
+  PackShape ps;
+  ps.count = raw.y;
+  ps.NP = raw.z & 0xffff;
+  ps.KP = (raw.z >> 16) & 0xff;
+  ps.LPS = (raw.z >> 24) & 0x7;
+  ps.NPq = (ps.NP + ps.LPS - 1) / ps.LPS;
+  return ps;
+}
+
 template <int KM, bool kSharedLaunch>
 __device__ __forceinline__ void fwd_pack(const FactorDev& F, const int4 raw, int lane, double* __restrict__ b,
                                          double* __restrict__ z) {
-  if (lane >= raw.y) return;
-  const int NP = raw.z & 0xffff, KP = raw.z >> 16;
-  const int4 meta = __ldg(F.pack_meta + (int64_t)(-1 - raw.x) * 32 + lane);
+  const PackShape ps = pack_shape(raw);
+  const int slot = lane / ps.LPS, g = lane - slot * ps.LPS;
+  if (slot >= ps.count) return;
+  const int4 meta = __ldg(F.pack_meta + (int64_t)(-1 - raw.x) * 32 + slot);
   const int c0 = meta.x, k = meta.y, nf = meta.z;
   const int32_t* R = F.rows + meta.w;
   // the supernode's own rows of b are final (its descendants sit on earlier levels) and no item
@@ -621,47 +641,64 @@ __device__ __forceinline__ void fwd_pack(const FactorDev& F, const int4 raw, int
   const double* V = F.pack_vals + (int64_t)raw.w * 32 + lane;
   // rows unrolled so that about 16 loads of each lane are in flight
 #pragma unroll(16 / KM)
-  for (int r = 0; r < NP; ++r) {
+  for (int rr = 0; rr < ps.NPq; ++rr) {
+    const int r = g + rr * ps.LPS;
     double acc = 0.0;
 #pragma unroll
     for (int j = 0; j < KM; ++j)
-      if (j < KP) acc = fma(__ldg(V + ((int64_t)j * NP + r) * 32), bv[j], acc);
+      if (j < ps.KP) acc = fma(__ldg(V + ((int64_t)j * ps.NPq + rr) * 32), bv[j], acc);
     if (r < k) z[c0 + r] = acc;
     else if (r < nf) atomicAdd(b + __ldg(R + (r - k)), -acc);
   }
 }
 
+// every lane of the warp runs this to the end (the partial sums of a supernode's lanes are
+// combined with warp shuffles)
 template <int KM, bool kSharedLaunch>
 __device__ __forceinline__ void bwd_pack(const FactorDev& F, const int4 raw, int lane, const double* __restrict__ z,
                                          double* __restrict__ x) {
-  if (lane >= raw.y) return;
-  const int NP = raw.z & 0xffff, KP = raw.z >> 16;
-  const int4 meta = __ldg(F.pack_meta + (int64_t)(-1 - raw.x) * 32 + lane);
-  const int c0 = meta.x, k = meta.y, nf = meta.z;
-  const int32_t* R = F.rows + meta.w;
+  const PackShape ps = pack_shape(raw);
+  const int slot = lane / ps.LPS, g = lane - slot * ps.LPS;
+  const bool active = slot < ps.count;
+  int c0 = 0, k = 0, nf = 0;
+  const int32_t* R = F.rows;
+  if (active) {
+    const int4 meta = __ldg(F.pack_meta + (int64_t)(-1 - raw.x) * 32 + slot);
+    c0 = meta.x;
+    k = meta.y;
+    nf = meta.z;
+    R = F.rows + meta.w;
+  }
   const double* V = F.pack_vals + (int64_t)raw.w * 32 + lane;
   double acc[KM];
 #pragma unroll
   for (int i = 0; i < KM; ++i) acc[i] = 0.0;
   // x_s = F11^T z_s - F21^T x_R: the ancestors' rows of x were written by earlier launches
 #pragma unroll(16 / KM)
-  for (int r = 0; r < NP; ++r) {
+  for (int rr = 0; rr < ps.NPq; ++rr) {
+    const int r = g + rr * ps.LPS;
     double v = 0.0;
     if (r < k) v = __ldg(z + c0 + r);
     else if (r < nf) v = -load_vec<kSharedLaunch>(x + __ldg(R + (r - k)));
 #pragma unroll
     for (int i = 0; i < KM; ++i)
-      if (i < KP) acc[i] = fma(__ldg(V + ((int64_t)i * NP + r) * 32), v, acc[i]);
+      if (i < ps.KP) acc[i] = fma(__ldg(V + ((int64_t)i * ps.NPq + rr) * 32), v, acc[i]);
   }
+  // the LPS lanes of a slot are adjacent and aligned: butterfly sums within them
+  for (int off = 1; off < ps.LPS; off <<= 1)
 #pragma unroll
-  for (int i = 0; i < KM; ++i)
-    if (i < k) x[c0 + i] = acc[i];
+    for (int i = 0; i < KM; ++i) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], off);
+  if (active && g == 0) {
+#pragma unroll
+    for (int i = 0; i < KM; ++i)
+      if (i < k) x[c0 + i] = acc[i];
+  }
 }
 
 template <bool kSharedLaunch>
 __device__ __forceinline__ void fwd_pack_any(const FactorDev& F, const int4 raw, int lane, double* __restrict__ b,
                                              double* __restrict__ z) {
-  const int KP = raw.z >> 16;
+  const int KP = (raw.z >> 16) & 0xff;
   if (KP <= 2) fwd_pack<2, kSharedLaunch>(F, raw, lane, b, z);
   else if (KP <= 4) fwd_pack<4, kSharedLaunch>(F, raw, lane, b, z);
   else fwd_pack<kPackMaxK, kSharedLaunch>(F, raw, lane, b, z);
@@ -670,7 +707,7 @@ __device__ __forceinline__ void fwd_pack_any(const FactorDev& F, const int4 raw,
 template <bool kSharedLaunch>
 __device__ __forceinline__ void bwd_pack_any(const FactorDev& F, const int4 raw, int lane,
                                              const double* __restrict__ z, double* __restrict__ x) {
-  const int KP = raw.z >> 16;
+  const int KP = (raw.z >> 16) & 0xff;
   if (KP <= 2) bwd_pack<2, kSharedLaunch>(F, raw, lane, z, x);
   else if (KP <= 4) bwd_pack<4, kSharedLaunch>(F, raw, lane, z, x);
   else bwd_pack<kPackMaxK, kSharedLaunch>(F, raw, lane, z, x);
@@ -1592,6 +1629,8 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
   if (tu.pdl < 0 || tu.pdl > 1) throw Error(JJA_ERR_ARG, "pdl must be 0 or 1");
   if (tu.pack_rows > 256) throw Error(JJA_ERR_ARG, "pack_rows must be <= 256");
   if (tu.pack_min_warps < 0) throw Error(JJA_ERR_ARG, "pack_min_warps must be >= 0");
+  if (tu.pack_lanes != 0 && tu.pack_lanes != 1 && tu.pack_lanes != 2 && tu.pack_lanes != 4)
+    throw Error(JJA_ERR_ARG, "pack_lanes must be 0, 1, 2 or 4");
   if (tu.groups < 0 || tu.groups > 64) throw Error(JJA_ERR_ARG, "groups must be in [0, 64]");
   const int WB = resolve_rhs_block(W, tu);
   if (w_hi < 0) w_hi = W;
@@ -1600,6 +1639,7 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
   // supernode)
   const int pack_rows = (W == 1 && tu.schedule != 2 && tu.pack_rows >= 0)
                             ? (tu.pack_rows ? tu.pack_rows : kDefaultPackRows) : 0;
+
   const int64_t pack_min_warps = tu.pack_min_warps ? tu.pack_min_warps : kDefaultPackMinWarps;
   const int target_warps = tu.target_warps ? tu.target_warps : kDefaultTargetWarps;
   const int min_piece = tu.min_piece ? tu.min_piece : kDefaultMinPiece;
@@ -1618,7 +1658,21 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
                            ? (tu.subtree_rows ? tu.subtree_rows : kDefaultSubRows) : 0;
   std::vector<int> level(F.sn_level.begin(), F.sn_level.end());
   std::vector<char> inside(F.ns, 0);
-  if (sub_rows > 0) build_subtrees(F, sub_rows, S, inside, level);
+  if (sub_rows > 0) {
+    build_subtrees(F, sub_rows, S, inside, level);
+    // by default only where the subtree launch has warps enough to hide each warp's walk (a
+    // subtree is walked member by member; the levels it replaces run its rows in parallel)
+    if (!tu.subtree_rows && (int64_t)S.subs.size() * ((W + 31) / 32) < kSubMinWarps) {
+      S.subs.clear();
+      S.sub_meta.clear();
+      S.sub_lrow.clear();
+      S.sub_loc.clear();
+      S.sub_max_rows = S.sub_max_f = S.sub_max_n = S.sub_max_l = 0;
+      S.n_levels = F.n_levels;
+      level.assign(F.sn_level.begin(), F.sn_level.end());
+      inside.assign(F.ns, 0);
+    }
+  }
   std::vector<std::vector<int>> by_level(S.n_levels);
   for (int s = 0; s < F.ns; ++s)
     if (!inside[s]) by_level[level[s]].push_back(s);
@@ -1678,19 +1732,25 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
     std::stable_sort(packable.begin(), packable.end(), [&](int a, int c) {
       return std::make_pair(F.sn_k[a], F.sn_m[a]) < std::make_pair(F.sn_k[c], F.sn_m[c]);
     });
-    for (size_t i = 0; i < packable.size(); i += 32) {
-      const int count = (int)std::min<size_t>(32, packable.size() - i);
+    // lanes per packed supernode: as tuned, else 4 on levels whose packs would give few warps at
+    // one lane each (more warps and shorter chains per lane), 1 on the others
+    const int lps = tu.pack_lanes ? tu.pack_lanes
+                                  : ((int64_t)(packable.size() + 31) / 32 < kPackLanesWarps ? 4 : 1);
+    const int per_pack = 32 / lps;
+    for (size_t i = 0; i < packable.size(); i += per_pack) {
+      const int count = (int)std::min<size_t>(per_pack, packable.size() - i);
       int NP = 0, KP = 0;
       for (int l = 0; l < count; ++l) {
         const int t = packable[i + l];
         NP = std::max(NP, F.sn_k[t] + F.sn_m[t]);
         KP = std::max(KP, F.sn_k[t]);
       }
+      const int NPq = (NP + lps - 1) / lps;
       const int64_t p = (int64_t)S.pack_sn.size() / 32, off = (int64_t)S.pack_vals.size() / 32;
       if (p >= INT32_MAX || off >= INT32_MAX) throw Error(JJA_ERR_ARG, "too many packed supernodes");
-      S.pack_vals.resize(S.pack_vals.size() + (size_t)32 * NP * KP, 0.0);
+      S.pack_vals.resize(S.pack_vals.size() + (size_t)32 * NPq * KP, 0.0);
       double* vals = S.pack_vals.data() + off * 32;
-      for (int l = 0; l < 32; ++l) {
+      for (int l = 0; l < 32; ++l) {   // slots: the first `count` of 32 entries
         if (l >= count) {
           S.pack_sn.push_back(-1);
           S.pack_meta.push_back(make_int4(0, 0, 0, 0));
@@ -1701,9 +1761,12 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
         S.pack_meta.push_back(make_int4(F.sn_col0[t], k, nf, (int)F.sn_rowptr[t]));
         const double* Fs = F.fcol.data() + F.sn_valptr[t];
         for (int j = 0; j < k; ++j)
-          for (int r = 0; r < nf; ++r) vals[((int64_t)j * NP + r) * 32 + l] = Fs[(int64_t)j * nf + r];
+          for (int r = 0; r < nf; ++r) {
+            const int lane = l * lps + r % lps, rr = r / lps;
+            vals[((int64_t)j * NPq + rr) * 32 + lane] = Fs[(int64_t)j * nf + r];
+          }
       }
-      const int4 item = make_int4((int)(-1 - p), count, NP | (KP << 16), (int)off);
+      const int4 item = make_int4((int)(-1 - p), count, NP | (KP << 16) | (lps << 24), (int)off);
       S.fi.push_back(item);
       S.bi.push_back(item);
     }

@@ -30,7 +30,7 @@ EXTRAP = {3: (2.0, -1.0), 4: (3.0, -3.0, 1.0), 5: (4.0, -6.0, 4.0, -1.0)}
 # launch-shape fields of the triangular solves (jja_solve_tuning)
 TUNING_FIELDS = ("rhs_block", "rows_per_lane", "target_warps", "min_piece", "schedule", "rows_per_lane_fwd",
                  "pack_rows", "pack_min_warps", "pdl", "groups", "coop_blocks", "dst_lines",
-                 "subtree_rows")
+                 "pack_lanes", "subtree_rows")
 SCHEDULES = {"levels": 1, "dataflow": 2, "cooperative": 3}
 
 

@@ -29,8 +29,13 @@ from .problem import TimeEvolutionProblem, TimeEvolutionResult, time_evolution
 __all__ = ["RaggedBatch"]
 
 PART_FROM_JUNCTIONS = 1 << 20    # batches of at least this many junctions (all copies) split in parts ...
-PART_JUNCTIONS = 1 << 22         # ... of about this many junctions each, 2 to MAX_PARTS of them
+PART_JUNCTIONS = 1 << 19         # ... of about this many junctions each, 2 to MAX_PARTS of them
 MAX_PARTS = 8
+# From this many junctions (all parts) the parts' packed levels take one lane per supernode: the
+# concurrent parts give the levels warps enough (measured on GB300, 31M junctions in 8 parts:
+# 4.80 ms per step with one lane, 4.99 with the library's per-level choice; 4.5M junctions in 8
+# parts: 0.91 against 0.82 ms)
+ONE_LANE_FROM_JUNCTIONS = 1 << 24
 _SEED_STRIDE = 0x632BE59BD9B4E019   # parts draw thermal noise from distinct Philox streams
 
 
@@ -63,8 +68,9 @@ def _geometry(c):
 
 def default_parts(n_junctions):
     """Concurrent parts of a batch with this many junctions (all copies): one union below 2^20
-    junctions, else one part per ~2^22 junctions, at least 2 and at most 8 (measured on GB300 with
-    4.5M junctions: one union 1.75 ms per step, two parts 1.17 ms)."""
+    junctions, else one part per ~2^19 junctions, at least 2 and at most 8 (measured on GB300 with
+    4.5M junctions: 2 parts 1.03 ms per step, 4 parts 0.86, 8 parts 0.80; 31M junctions: 8 parts
+    5.1 ms, 12 parts 5.2, 16 parts 5.5)."""
     if n_junctions < PART_FROM_JUNCTIONS:
         return 1
     return int(min(MAX_PARTS, max(2, -(-n_junctions // PART_JUNCTIONS))))
@@ -204,6 +210,9 @@ class RaggedBatch:
         from .backend import GpuSimulation, _torch
         if options.get("device") is None:   # the caller's device, not each new thread's default
             options = dict(options, device=_torch().cuda.current_device())
+        if self.Nj >= ONE_LANE_FROM_JUNCTIONS and not (options.get("tuning") or {}).get("pack_lanes"):
+            # the parts' concurrent levels already hold many warps: one lane per packed supernode
+            options = dict(options, tuning=dict(options.get("tuning") or {}, pack_lanes=1))
         sims = [None] * len(self.parts)
 
         def build(k):      # the parts' factorisations and plan uploads run in parallel host threads

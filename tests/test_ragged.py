@@ -55,7 +55,10 @@ def test_union_layout_with_oracle_core(parts):
 
 
 def test_default_parts():
+    from pyjjasim_gb300.ragged import default_parts
     assert len(RaggedBatch(_problems()).parts) == 1       # small batches stay one union
+    # one part per ~2^19 junctions from 2^20 junctions on, 2 to 8 of them
+    assert [default_parts(n) for n in (980588, 1 << 20, 1200000, 4530208, 30964399)] == [1, 2, 3, 8, 8]
 
 
 def test_mismatched_problems_rejected():

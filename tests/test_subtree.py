@@ -28,11 +28,20 @@ def _factor(c, W, ordering):
 def test_schedule_with_subtrees(lattice, n, ordering):
     f = _factor(LATTICES[lattice](n, n), 64, ordering)
     n_off = f.check_schedule(64, {"subtree_rows": -1})
-    for rows in (0, 8, 32, 64):
+    for rows in (8, 32, 64):
         n_on = f.check_schedule(64, {"subtree_rows": rows})
         assert n_on[0] < n_off[0] and n_on[1] <= n_off[1]
     # below 32 problems per warp no subtrees are built
-    assert f.check_schedule(8, {}) == f.check_schedule(8, {"subtree_rows": -1})
+    assert f.check_schedule(8, {"subtree_rows": 32}) == f.check_schedule(8, {"subtree_rows": -1})
+
+
+def test_default_takes_subtrees_where_the_launch_is_wide():
+    # SquareArray(128,128): about 1000 subtrees, so W = 512 (16 warps each) takes them by default
+    # and W = 32 (one warp each, fewer than 152 x 16 warps in all) does not
+    f = _factor(SquareArray(128, 128), 512, "mmd")
+    assert f.check_schedule(512, {}) == f.check_schedule(512, {"subtree_rows": 32})
+    assert f.check_schedule(512, {}) != f.check_schedule(512, {"subtree_rows": -1})
+    assert f.check_schedule(32, {}) == f.check_schedule(32, {"subtree_rows": -1})
 
 
 def test_subtree_rows_bound():
