@@ -23,6 +23,7 @@
 #include <stdexcept>
 #include <string>
 #include <mutex>
+#include <map>
 #include <vector>
 
 namespace {
@@ -81,6 +82,9 @@ constexpr int kNumSMs = 152;                     // GB300
 constexpr int kDefaultTargetWarps = 152 * 24;   // levels with fewer work items split their dot products
 constexpr int kDefaultMinPiece = 16;     // shortest piece of a split dot product
 constexpr int kDefaultSubRows = 32;     // subtree sweeps: rows per subtree (columns + the root's off-diagonal rows)
+constexpr int kSubMaxRows = 64;          // ... at most this many rows (tuning bound)
+constexpr int kDefaultSubRows1 = 16;     // ... at W = 1 (subtree packs)
+constexpr int kSubPackMinWarps = 152 * 4;   // ... by default at W = 1 from this many warps
 constexpr int kSubMinWarps = 152 * 16;  // ... by default only when the launch has at least this many warps
 constexpr int kSubMaxWarps = 8;         // ... warps (32-problem blocks of one subtree) per block
 constexpr int kSubMaxK = 8;             // ... members of at most this many columns
@@ -911,10 +915,18 @@ __host__ __device__ inline size_t sub_smem_bytes(const SubDev& S, int warps) {
          (size_t)S.max_n * (sizeof(int4) + sizeof(int32_t)) + (size_t)S.max_l * sizeof(uint16_t);
 }
 
+// F value idx of a member: staged in shared memory (FS = 1) or interleaved by lane in global
+// memory (FS = 32, the W = 1 subtree packs)
+template <int FS>
+__device__ __forceinline__ double sub_f(const double* Fr, int idx) {
+  if (FS == 1) return Fr[idx];
+  return __ldg(Fr + (int64_t)idx * FS);
+}
+
 // forward, one member with K columns: z rows from the buffer's b rows, then its off-diagonal
 // rows updated in the buffer (b_R -= F21 b_s). `buf` points at this lane's row 0 (rows 32
 // doubles apart), `zs` at z row c0 + c of this lane's problem.
-template <int K>
+template <int K, int FS = 1>
 __device__ __forceinline__ void sub_fwd_member(const double* Fr, const uint16_t* L, int c, int nf, double* buf,
                                                double* zs, int64_t W) {
   double bs[K];
@@ -924,7 +936,7 @@ __device__ __forceinline__ void sub_fwd_member(const double* Fr, const uint16_t*
   for (int r = 0; r < K; ++r) {
     double acc = 0.0;
 #pragma unroll
-    for (int j = 0; j <= r; ++j) acc = fma(Fr[r * K + j], bs[j], acc);
+    for (int j = 0; j <= r; ++j) acc = fma(sub_f<FS>(Fr, r * K + j), bs[j], acc);
     zs[(int64_t)r * W] = acc;
   }
   // two rows at a time: a member's off-diagonal rows are distinct, so both loads go first
@@ -934,8 +946,8 @@ __device__ __forceinline__ void sub_fwd_member(const double* Fr, const uint16_t*
     double t0 = buf[l0 * 32], t1 = buf[l1 * 32];
 #pragma unroll
     for (int j = 0; j < K; ++j) {
-      t0 = fma(-Fr[r * K + j], bs[j], t0);
-      t1 = fma(-Fr[(r + 1) * K + j], bs[j], t1);
+      t0 = fma(-sub_f<FS>(Fr, r * K + j), bs[j], t0);
+      t1 = fma(-sub_f<FS>(Fr, (r + 1) * K + j), bs[j], t1);
     }
     buf[l0 * 32] = t0;
     buf[l1 * 32] = t1;
@@ -944,7 +956,7 @@ __device__ __forceinline__ void sub_fwd_member(const double* Fr, const uint16_t*
     const int l0 = L[r - K];
     double t0 = buf[l0 * 32];
 #pragma unroll
-    for (int j = 0; j < K; ++j) t0 = fma(-Fr[r * K + j], bs[j], t0);
+    for (int j = 0; j < K; ++j) t0 = fma(-sub_f<FS>(Fr, r * K + j), bs[j], t0);
     buf[l0 * 32] = t0;
   }
 }
@@ -952,7 +964,7 @@ __device__ __forceinline__ void sub_fwd_member(const double* Fr, const uint16_t*
 // backward, one member: x_s = inv(L11)^T z_s - (L21 inv(L11))^T x_R with z_s in the buffer's
 // own rows and x_R in its ancestors' rows (computed before, or loaded for the root's rows);
 // x_s replaces z_s in the buffer and goes to x row c0 + c (`xs`)
-template <int K>
+template <int K, int FS = 1>
 __device__ __forceinline__ void sub_bwd_member(const double* Fr, const uint16_t* L, int c, int nf, double* buf,
                                                double* xs, int64_t W) {
   double acc[K];
@@ -962,19 +974,44 @@ __device__ __forceinline__ void sub_bwd_member(const double* Fr, const uint16_t*
   for (int r = 0; r < K; ++r) {
     const double zr = buf[(c + r) * 32];
 #pragma unroll
-    for (int j = 0; j <= r; ++j) acc[j] = fma(Fr[r * K + j], zr, acc[j]);
+    for (int j = 0; j <= r; ++j) acc[j] = fma(sub_f<FS>(Fr, r * K + j), zr, acc[j]);
   }
 #pragma unroll 4
   for (int r = K; r < nf; ++r) {
     const double xr = buf[L[r - K] * 32];
 #pragma unroll
-    for (int j = 0; j < K; ++j) acc[j] = fma(-Fr[r * K + j], xr, acc[j]);
+    for (int j = 0; j < K; ++j) acc[j] = fma(-sub_f<FS>(Fr, r * K + j), xr, acc[j]);
   }
 #pragma unroll
   for (int j = 0; j < K; ++j) {
     buf[(c + j) * 32] = acc[j];
     xs[(int64_t)j * W] = acc[j];
   }
+}
+
+// one member of a subtree walk: the K-specialised walker of its width
+template <bool kForward, int FS>
+__device__ __forceinline__ void sub_member(int k, const double* Fr, const uint16_t* L, int c, int nf, double* buf,
+                                           double* out, int64_t W) {
+#define JJA_SUB_CASE(KK)                                                  \
+  case KK:                                                                \
+    if (kForward) sub_fwd_member<KK, FS>(Fr, L, c, nf, buf, out, W);     \
+    else sub_bwd_member<KK, FS>(Fr, L, c, nf, buf, out, W);              \
+    break;
+  switch (k) {
+    JJA_SUB_CASE(1)
+    JJA_SUB_CASE(2)
+    JJA_SUB_CASE(3)
+    JJA_SUB_CASE(4)
+    JJA_SUB_CASE(5)
+    JJA_SUB_CASE(6)
+    JJA_SUB_CASE(7)
+    default:
+      if (kForward) sub_fwd_member<8, FS>(Fr, L, c, nf, buf, out, W);
+      else sub_bwd_member<8, FS>(Fr, L, c, nf, buf, out, W);
+      break;
+  }
+#undef JJA_SUB_CASE
 }
 
 // grid (subtrees, ceil(problem blocks / warps per block)); block = warps per block x 32.
@@ -1012,17 +1049,7 @@ __global__ void __launch_bounds__(256) k_subtree(FactorDev F, SubDev S, int W, i
       const int4 mt = Msh[i];
       const double* Fr = Fsh + mt.w;
       const uint16_t* L = Lsh + Lrow[i];
-      double* zs = z + (int64_t)(T.c0 + mt.x) * Wl + w;
-      switch (mt.y) {
-        case 1: sub_fwd_member<1>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
-        case 2: sub_fwd_member<2>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
-        case 3: sub_fwd_member<3>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
-        case 4: sub_fwd_member<4>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
-        case 5: sub_fwd_member<5>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
-        case 6: sub_fwd_member<6>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
-        case 7: sub_fwd_member<7>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
-        default: sub_fwd_member<8>(Fr, L, mt.x, mt.z, buf, zs, Wl); break;
-      }
+      sub_member<true, 1>(mt.y, Fr, L, mt.x, mt.z, buf, z + (int64_t)(T.c0 + mt.x) * Wl + w, Wl);
     }
     for (int q = 0; q < T.m_root; ++q) atomicAdd(b + (int64_t)__ldg(R + q) * Wl + w, buf[(T.ncols + q) * 32]);
   } else {
@@ -1034,17 +1061,71 @@ __global__ void __launch_bounds__(256) k_subtree(FactorDev F, SubDev S, int W, i
       const int4 mt = Msh[i];
       const double* Fr = Fsh + mt.w;
       const uint16_t* L = Lsh + Lrow[i];
-      double* xs = x + (int64_t)(T.c0 + mt.x) * Wl + w;
-      switch (mt.y) {
-        case 1: sub_bwd_member<1>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
-        case 2: sub_bwd_member<2>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
-        case 3: sub_bwd_member<3>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
-        case 4: sub_bwd_member<4>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
-        case 5: sub_bwd_member<5>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
-        case 6: sub_bwd_member<6>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
-        case 7: sub_bwd_member<7>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
-        default: sub_bwd_member<8>(Fr, L, mt.x, mt.z, buf, xs, Wl); break;
-      }
+      sub_member<false, 1>(mt.y, Fr, L, mt.x, mt.z, buf, x + (int64_t)(T.c0 + mt.x) * Wl + w, Wl);
+    }
+  }
+}
+
+// W = 1 subtree packs: subtrees of one shape (the same members, widths, heights and local row
+// maps; the bottoms of lattices repeat a few hundred shapes) are grouped 32 to a warp, one per
+// lane, with their F values interleaved by lane (the load of a value index is 256 contiguous
+// bytes). Each lane walks its subtree as k_subtree's lanes walk theirs, on its own column of the
+// warp's shared buffer; the shape's metadata and row maps are the same for every lane.
+struct SubShape {
+  int n, ncols, m_root, f_len;   // members, columns, root rows, F values per subtree
+  int meta_off, pad;             // into meta and lrow (per member)
+  int64_t loc_off;               // into loc
+};
+
+struct SubPackDev {
+  const int4* items = nullptr;     // per warp: shape, subtrees (lanes), first lane slot, F values offset / 32
+  const SubShape* shapes = nullptr;
+  const int4* meta = nullptr;      // per member of a shape: column, k, k + m, F offset (in the subtree)
+  const int32_t* lrow = nullptr;   // per member of a shape: offset of its row map in the shape's loc
+  const uint16_t* loc = nullptr;
+  const int32_t* c0 = nullptr;     // per lane slot: the subtree's first column
+  const int64_t* roff = nullptr;   // per lane slot: its root's rows in F.rows
+  const double* vals = nullptr;    // F values, interleaved by lane
+  int n_items = 0, max_rows = 0;
+};
+
+constexpr int kSubPackWarps = 4;   // warps per block (independent items)
+
+template <bool kForward>
+__global__ void __launch_bounds__(kSubPackWarps * 32) k_subtree_pack(FactorDev F, SubPackDev P, double* __restrict__ b,
+                                                                    double* __restrict__ z, double* __restrict__ x) {
+  pdl_begin();
+  extern __shared__ double subp_sh[];
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int it = blockIdx.x * kSubPackWarps + wi;
+  if (it >= P.n_items) return;
+  const int4 item = P.items[it];
+  if (lane >= item.y) return;   // lanes walk independently: no warp-level synchronisation below
+  const SubShape T = P.shapes[item.x];
+  double* buf = subp_sh + (size_t)wi * P.max_rows * 32 + lane;
+  const int c0 = __ldg(P.c0 + item.z + lane);
+  const int32_t* R = F.rows + __ldg(P.roff + item.z + lane);
+  const double* V = P.vals + (int64_t)item.w * 32 + lane;
+  const uint16_t* loc = P.loc + T.loc_off;
+  if (kForward) {
+#pragma unroll 4
+    for (int i = 0; i < T.ncols; ++i) buf[i * 32] = b[c0 + i];
+    for (int q = 0; q < T.m_root; ++q) buf[(T.ncols + q) * 32] = 0.0;
+    for (int i = 0; i < T.n; ++i) {
+      const int4 mt = __ldg(P.meta + T.meta_off + i);
+      sub_member<true, 32>(mt.y, V + (int64_t)mt.w * 32, loc + __ldg(P.lrow + T.meta_off + i), mt.x, mt.z, buf,
+                           z + c0 + mt.x, 1);
+    }
+    for (int q = 0; q < T.m_root; ++q) atomicAdd(b + __ldg(R + q), buf[(T.ncols + q) * 32]);
+  } else {
+#pragma unroll 4
+    for (int q = 0; q < T.m_root; ++q) buf[(T.ncols + q) * 32] = __ldcg(x + __ldg(R + q));
+#pragma unroll 4
+    for (int i = 0; i < T.ncols; ++i) buf[i * 32] = __ldg(z + c0 + i);
+    for (int i = T.n - 1; i >= 0; --i) {
+      const int4 mt = __ldg(P.meta + T.meta_off + i);
+      sub_member<false, 32>(mt.y, V + (int64_t)mt.w * 32, loc + __ldg(P.lrow + T.meta_off + i), mt.x, mt.z, buf,
+                            x + c0 + mt.x, 1);
     }
   }
 }
@@ -1513,6 +1594,15 @@ struct Schedule {
   std::vector<int32_t> sub_lrow;
   std::vector<uint16_t> sub_loc;
   int sub_max_rows = 0, sub_max_f = 0, sub_max_n = 0, sub_max_l = 0;
+  // W = 1: the subtrees grouped by shape into warps (k_subtree_pack; the tables above are then
+  // empty)
+  std::vector<int4> sp_items, sp_meta;
+  std::vector<SubShape> sp_shapes;
+  std::vector<int32_t> sp_lrow, sp_c0;
+  std::vector<uint16_t> sp_loc;
+  std::vector<int64_t> sp_roff;
+  std::vector<double> sp_vals;
+  int sp_max_rows = 0;
 };
 
 // the supernodes a work item covers: one, or the members of a W = 1 pack
@@ -1615,6 +1705,74 @@ void build_subtrees(const jja::Factor& F, int max_rows, Schedule& S, std::vector
   S.n_levels = top + 1;
 }
 
+// W = 1: the subtrees of S (build_subtrees) grouped 32 to a warp by shape: equal member count,
+// columns, root rows, per-member (column, k, k + m, F offset, row-map offset) and row maps, so a
+// warp's lanes run the same walk; their F values (row-major per member) interleaved by lane.
+// Replaces S's per-subtree tables.
+void build_subtree_packs(const jja::Factor& F, Schedule& S) {
+  std::map<std::vector<int>, std::vector<int>> by_shape;
+  for (int t = 0; t < (int)S.subs.size(); ++t) {
+    const SubTree& T = S.subs[t];
+    std::vector<int> sig = {T.n, T.ncols, T.m_root, T.f_len, T.l_len};
+    for (int u = T.s0; u < T.s0 + T.n; ++u) {
+      const int4 mt = S.sub_meta[u];
+      sig.insert(sig.end(), {mt.x, mt.y, mt.z, mt.w, S.sub_lrow[u]});
+    }
+    for (int64_t q = 0; q < T.l_len; ++q) sig.push_back(S.sub_loc[T.l_off + q]);
+    by_shape[sig].push_back(t);
+  }
+  for (const auto& kv : by_shape) {
+    const std::vector<int>& ts = kv.second;
+    const SubTree& T0 = S.subs[ts[0]];
+    SubShape sh{};
+    sh.n = T0.n;
+    sh.ncols = T0.ncols;
+    sh.m_root = T0.m_root;
+    sh.f_len = T0.f_len;
+    sh.meta_off = (int)S.sp_meta.size();
+    sh.loc_off = (int64_t)S.sp_loc.size();
+    for (int u = T0.s0; u < T0.s0 + T0.n; ++u) {
+      S.sp_meta.push_back(S.sub_meta[u]);
+      S.sp_lrow.push_back(S.sub_lrow[u]);
+    }
+    S.sp_loc.insert(S.sp_loc.end(), S.sub_loc.begin() + T0.l_off, S.sub_loc.begin() + T0.l_off + T0.l_len);
+    const int shape = (int)S.sp_shapes.size();
+    S.sp_shapes.push_back(sh);
+    S.sp_max_rows = std::max(S.sp_max_rows, sh.ncols + sh.m_root);
+    for (size_t i = 0; i < ts.size(); i += 32) {
+      const int count = (int)std::min<size_t>(32, ts.size() - i);
+      const int64_t lane0 = (int64_t)S.sp_c0.size(), off = (int64_t)S.sp_vals.size() / 32;
+      if (lane0 >= INT32_MAX || off >= INT32_MAX) throw Error(JJA_ERR_ARG, "too many subtree packs");
+      S.sp_vals.resize(S.sp_vals.size() + (size_t)32 * sh.f_len, 0.0);
+      double* vals = S.sp_vals.data() + off * 32;
+      for (int l = 0; l < 32; ++l) {
+        if (l >= count) {
+          S.sp_c0.push_back(0);
+          S.sp_roff.push_back(0);
+          continue;
+        }
+        const SubTree& T = S.subs[ts[i + l]];
+        S.sp_c0.push_back(T.c0);
+        S.sp_roff.push_back(T.r_off);
+        // F row-major per member, at the member's offset in the subtree
+        for (int u = T.s0; u < T.s0 + T.n; ++u) {
+          const int k = F.sn_k[u], nf = k + F.sn_m[u];
+          const double* src = F.fcol.data() + F.sn_valptr[u];
+          const int64_t f = F.sn_valptr[u] - T.f_off;
+          for (int r = 0; r < nf; ++r)
+            for (int j = 0; j < k; ++j) vals[(f + (int64_t)r * k + j) * 32 + l] = src[(int64_t)j * nf + r];
+        }
+      }
+      S.sp_items.push_back(make_int4(shape, count, (int)lane0, (int)off));
+    }
+  }
+  S.subs.clear();
+  S.sub_meta.clear();
+  S.sub_lrow.clear();
+  S.sub_loc.clear();
+  S.sub_max_rows = S.sub_max_f = S.sub_max_n = S.sub_max_l = 0;
+}
+
 // the work items of problems [w_lo, w_hi) (w_hi < 0: all W); w_lo a multiple of the RHS block
 Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu, int w_lo = 0, int w_hi = -1) {
   if (W <= 0 || W >= (1 << 30)) throw Error(JJA_ERR_ARG, "W must be in [1, 2^30)");
@@ -1625,7 +1783,7 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
   if (tu.schedule < 0 || tu.schedule > 3) throw Error(JJA_ERR_ARG, "schedule must be 0, 1, 2 or 3");
   if (tu.coop_blocks < 0) throw Error(JJA_ERR_ARG, "coop_blocks must be >= 0");
   if (tu.dst_lines < 0 || tu.dst_lines > 2) throw Error(JJA_ERR_ARG, "dst_lines must be 0, 1 or 2");
-  if (tu.subtree_rows > 64) throw Error(JJA_ERR_ARG, "subtree_rows must be <= 64");
+  if (tu.subtree_rows > kSubMaxRows) throw Error(JJA_ERR_ARG, "subtree_rows must be <= 64");
   if (tu.pdl < 0 || tu.pdl > 1) throw Error(JJA_ERR_ARG, "pdl must be 0 or 1");
   if (tu.pack_rows > 256) throw Error(JJA_ERR_ARG, "pack_rows must be <= 256");
   if (tu.pack_min_warps < 0) throw Error(JJA_ERR_ARG, "pack_min_warps must be >= 0");
@@ -1654,15 +1812,15 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
   }
   // subtree sweeps at the bottom of the tree (level schedule, 32 problems per warp); the other
   // supernodes are re-levelled above them
-  const int sub_rows = (WB == 32 && tu.schedule <= 1 && tu.subtree_rows >= 0)
-                           ? (tu.subtree_rows ? tu.subtree_rows : kDefaultSubRows) : 0;
+  const int sub_rows = ((WB == 32 || W == 1) && tu.schedule <= 1 && tu.subtree_rows >= 0)
+                           ? (tu.subtree_rows ? tu.subtree_rows : (W == 1 ? kDefaultSubRows1 : kDefaultSubRows)) : 0;
   std::vector<int> level(F.sn_level.begin(), F.sn_level.end());
   std::vector<char> inside(F.ns, 0);
   if (sub_rows > 0) {
     build_subtrees(F, sub_rows, S, inside, level);
     // by default only where the subtree launch has warps enough to hide each warp's walk (a
     // subtree is walked member by member; the levels it replaces run its rows in parallel)
-    if (!tu.subtree_rows && (int64_t)S.subs.size() * ((W + 31) / 32) < kSubMinWarps) {
+    if (W > 1 && !tu.subtree_rows && (int64_t)S.subs.size() * ((W + 31) / 32) < kSubMinWarps) {
       S.subs.clear();
       S.sub_meta.clear();
       S.sub_lrow.clear();
@@ -1671,6 +1829,18 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
       S.n_levels = F.n_levels;
       level.assign(F.sn_level.begin(), F.sn_level.end());
       inside.assign(F.ns, 0);
+    }
+    if (W == 1) {
+      build_subtree_packs(F, S);
+      // by default only where the packs fill warps enough (a few hundred subtree packs walk
+      // slower than the levels they replace)
+      if (!tu.subtree_rows && (int64_t)S.sp_items.size() < kSubPackMinWarps) {
+        S = Schedule{};
+        S.n_levels = F.n_levels;
+        S.ns = F.ns;
+        level.assign(F.sn_level.begin(), F.sn_level.end());
+        inside.assign(F.ns, 0);
+      }
     }
   }
   std::vector<std::vector<int>> by_level(S.n_levels);
@@ -1977,6 +2147,7 @@ struct jja_plan {
   bool coop_packs = false;
   // fast Poisson solve of uniform square arrays (jja_plan_set_fast_poisson): replaces both sweeps
   SubDev sub{};        // subtree sweeps (k_subtree; n = 0: none)
+  SubPackDev subp{};   // W = 1 subtree packs (k_subtree_pack; n_items = 0: none)
   int dst = 0;
   int dst_lines = 0;   // grid lines per block of the sine-transform kernels (0: by grid size)
   DstArgs dst_args{};
@@ -2137,6 +2308,12 @@ void launch_coop(jja_plan* p, cudaStream_t st, bool forward, double* b, double* 
 
 // the subtree sweep of group g (before the forward levels, after the backward ones)
 void launch_subtrees(jja_plan* p, const Group& g, cudaStream_t st, bool forward, double* b, double* z, double* x) {
+  if (p->subp.n_items) {
+    const int grid = (p->subp.n_items + kSubPackWarps - 1) / kSubPackWarps;
+    const size_t smem = (size_t)kSubPackWarps * p->subp.max_rows * 32 * sizeof(double);
+    launch_smem(p->pdl, forward ? k_subtree_pack<true> : k_subtree_pack<false>, dim3((unsigned)grid),
+                kSubPackWarps * 32, smem, st, p->F, p->subp, b, z, x);
+  }
   if (!p->sub.n) return;
   const int blocks = (g.wn + 31) / 32;
   const int warps = std::min(blocks, kSubMaxWarps);
@@ -2564,6 +2741,23 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
       JJA_CUDA(cudaMemset(g.d_step, 0, 4 * sizeof(int64_t)));
     };
     set_group(p->all, S, 0, d->W);
+    if (!S.sp_items.empty()) {
+      SubPackDev& sp = p->subp;
+      sp.items = p->up(S.sp_items.data(), S.sp_items.size());
+      sp.shapes = p->up(S.sp_shapes.data(), S.sp_shapes.size());
+      sp.meta = p->up(S.sp_meta.data(), S.sp_meta.size());
+      sp.lrow = p->up(S.sp_lrow.data(), S.sp_lrow.size());
+      sp.loc = p->up(S.sp_loc.data(), S.sp_loc.size());
+      sp.c0 = p->up(S.sp_c0.data(), S.sp_c0.size());
+      sp.roff = p->up(S.sp_roff.data(), S.sp_roff.size());
+      sp.vals = p->up(S.sp_vals.data(), S.sp_vals.size());
+      sp.n_items = (int)S.sp_items.size();
+      sp.max_rows = S.sp_max_rows;
+      // the attribute is the kernel's, shared by every plan: the largest any plan can need
+      const int smem = (int)((size_t)kSubPackWarps * kSubMaxRows * 32 * sizeof(double));
+      JJA_CUDA(cudaFuncSetAttribute(k_subtree_pack<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      JJA_CUDA(cudaFuncSetAttribute(k_subtree_pack<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    }
     if (!S.subs.empty()) {
       SubDev& sd = p->sub;
       sd.tab = p->up(S.subs.data(), S.subs.size());
@@ -2575,8 +2769,15 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
       sd.max_f = S.sub_max_f;
       sd.max_n = S.sub_max_n;
       sd.max_l = S.sub_max_l;
-      const size_t smem = sub_smem_bytes(sd, kSubMaxWarps);
-      if (smem > (size_t)227 * 1024) throw Error(JJA_ERR_INTERNAL, "subtree staging exceeds shared memory");
+      // the attribute is the kernel's, shared by every plan: the largest any plan can need
+      SubDev bound{};
+      bound.max_rows = kSubMaxRows;
+      bound.max_f = kSubMaxF;
+      bound.max_n = kSubMaxRows;
+      bound.max_l = kSubMaxL;
+      const size_t smem = sub_smem_bytes(bound, kSubMaxWarps);
+      if (sub_smem_bytes(sd, kSubMaxWarps) > smem || smem > (size_t)227 * 1024)
+        throw Error(JJA_ERR_INTERNAL, "subtree staging exceeds shared memory");
       JJA_CUDA(cudaFuncSetAttribute(k_subtree<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       JJA_CUDA(cudaFuncSetAttribute(k_subtree<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }

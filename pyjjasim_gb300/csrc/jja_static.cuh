@@ -667,6 +667,7 @@ int jja_static_create(const jja_static_desc* d, const jja_factor* fac, jja_stati
     // W = 1 sweep items (no lane packs: every problem has its own factor values)
     jja_solve_tuning tu{};
     tu.pack_rows = -1;
+    tu.subtree_rows = -1;   // the static sweeps run level items only
     tu.rows_per_lane = 1;
     const Schedule Sch = build_schedule(F, 1, tu);
     sp->fwd_ptr = Sch.fwd_ptr;

@@ -151,14 +151,17 @@ def test_dataflow_schedule_waits_only_on_earlier_items(make, ordering, W, tuning
     A, K = P.face_matrix(c, 0.05)
     coords, perm = P.fill_reducing_order(K, ordering, c)
     f = P.HostFactor(K, coords=coords, perm=perm)
-    nf, nb = f.check_schedule(W, tuning)
+    nf, nb = f.check_schedule(W, tuning)          # with the library's subtree sweeps
+    assert nf >= 0 and nb >= 0
+    # without subtrees every supernode has a level item, or a place in a W = 1 pack of <= 32
+    flat = dict(tuning or {}, subtree_rows=-1)
+    nf, nb = f.check_schedule(W, flat)
     ns = f.stats["n_supernodes"]
-    # a W = 1 pack holds up to 32 small supernodes; otherwise every supernode has >= 1 item
-    packed = W == 1 and (tuning or {}).get("pack_rows", 0) >= 0
+    packed = W == 1 and flat.get("pack_rows", 0) >= 0
     least = -(-ns // 32) if packed else ns
     assert nf >= least and nb >= least
-    if packed and (tuning or {}).get("pack_min_warps") == 1 and ns > 64:   # packs on every level
-        nf1, nb1 = f.check_schedule(W, {"pack_rows": -1})
+    if packed and flat.get("pack_min_warps") == 1 and ns > 64:   # packs on every level
+        nf1, nb1 = f.check_schedule(W, {"pack_rows": -1, "subtree_rows": -1})
         assert nf < nf1 and nb < nb1
 
 

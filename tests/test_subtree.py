@@ -68,6 +68,47 @@ def test_subtree_solve_matches_scipy(lattice, n, W, ordering, rows):
     assert float(np.abs(x - ref).max()) <= 1e-11 * float(np.abs(ref).max())
 
 
+def test_w1_schedule_packs_subtrees_by_shape():
+    # W = 1: subtrees of one shape share a warp (32 per warp); the remaining levels shrink
+    f = _factor(SquareArray(96, 96), 1, "nd")
+    n_off = f.check_schedule(1, {"subtree_rows": -1})
+    for rows in (16, 32, 64):
+        n_on = f.check_schedule(1, {"subtree_rows": rows})
+        assert n_on[0] < n_off[0] and n_on[1] < n_off[1]
+    # by default only where the packs fill 152 x 4 warps: not for this single array
+    assert f.check_schedule(1, {}) == n_off
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lattice,n,ordering", [("square", 96, "nd"), ("honeycomb", 40, "mmd"),
+                                                ("triangular", 48, "nd")])
+@pytest.mark.parametrize("rows", [0, 16, 64, -1])
+def test_w1_subtree_packs_solve_matches_scipy(lattice, n, ordering, rows):
+    c = LATTICES[lattice](n, n)
+    c.set_inductance(0.03)
+    A, K = P.face_matrix(c, 0.05)
+    b = _rhs(K, 1, n + rows)[:, 0]
+    x = backend.solve_faces(c, 0.05, b, ordering=ordering, tuning={"subtree_rows": rows})
+    ref = scipy.sparse.linalg.spsolve(K.tocsc(), b)
+    assert float(np.abs(x - ref).max()) <= 1e-11 * float(np.abs(ref).max())
+
+
+@pytest.mark.gpu
+def test_w1_ragged_union_with_and_without_subtree_packs():
+    from pyjjasim_gb300.ragged import RaggedBatch
+    probs = []
+    for k, lat in enumerate((SquareArray, HoneycombArray, TriangularArray, SquareArray)):
+        cc = lat(24 + 6 * k, 20 + 4 * k)
+        Is = cc.current_base(0.0)[:, None, None] * np.array([0.7 + 0.2 * k])[None, :, None]
+        probs.append(TimeEvolutionProblem(cc, time_step=0.05, time_step_count=120, current_sources=Is,
+                                          external_flux=0.15, store_time_steps=[119]))
+    rb = RaggedBatch(probs, parts=1)
+    th_on = [r.get_theta() for r in rb.compute(tuning={"subtree_rows": 32})]
+    th_off = [r.get_theta() for r in rb.compute(tuning={"subtree_rows": -1})]
+    for a, b in zip(th_on, th_off):
+        assert float(np.abs(a - b).max()) <= 1e-11 * max(1.0, float(np.abs(b).max()))
+
+
 @pytest.mark.gpu
 def test_trajectories_with_and_without_subtrees_agree():
     c = SquareArray(48, 48)
