@@ -628,6 +628,20 @@ def profile_mode(args):
         ok = bool(sim.plan.fast_poisson) and bool(torch.isfinite(sim.theta()).all())
         print(json.dumps({"profile_case": "fast_poisson", "steps": 3 + args.profile_steps, "ok": ok}))
         sys.exit(0 if ok else 1)
+    if args.profile_case == "large":
+        # the large single array's step: SquareArray(1024,1024), C = 0.5, L = 0.05, W = 8 (sources
+        # zero: the kernels' cost does not depend on the values)
+        a = G.SquareArray(1024, 1024)
+        a.set_capacitance(0.5)
+        a.set_inductance(0.05)
+        bias = np.zeros((a.junction_count(), 8, 1))
+        p = G.TimeEvolutionProblem(a, time_step=0.05, time_step_count=10 ** 6, external_flux=0.1, current_sources=bias)
+        sim = GpuSimulation(p)
+        sim.run(3 + args.profile_steps, use_graph=False)
+        sim.synchronize()
+        ok = bool(torch.isfinite(sim.theta()).all())
+        print(json.dumps({"profile_case": "large", "W": 8, "steps": 3 + args.profile_steps, "ok": ok}))
+        sys.exit(0 if ok else 1)
     if args.profile_case == "ragged":
         # the W = 1 level kernels on a block-diagonal union: the first 8 problems of the ragged
         # draws as one part (sources zero: the kernels' cost does not depend on the values)
@@ -677,9 +691,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--profile-case", default="iv", choices=["iv", "fast_poisson", "static", "ragged"],
+    ap.add_argument("--profile-case", default="iv", choices=["iv", "fast_poisson", "static", "ragged", "large"],
                     help="profiling mode: the IV sweep (default), the fast Poisson single array, the static "
-                         "solver, the W = 1 ragged union")
+                         "solver, the W = 1 ragged union, the 1024x1024 x 8 array")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling mode: plan, 3 eager warm-up steps, then this many eager steps, nothing else")
     ap.add_argument("--W", type=int, default=W_BATCH, help="problems per launch (profiling mode)")

@@ -112,13 +112,16 @@ typedef struct {
   int pack_lanes;     /* W = 1 packs: lanes per packed supernode, 1, 2 or 4 (its rows split between
                          them; 32 / pack_lanes supernodes per warp); 0: default (per level: 4 where
                          one lane per supernode would give fewer than 4096 warps, else 1) */
-  int subtree_rows;   /* level schedule with 32 problems per warp (W >= 17): subtrees at the bottom of
-                         the elimination tree spanning at most this many rows (their columns plus
-                         their root's off-diagonal rows, <= 64) are solved one warp per subtree and
-                         32 problems in shared memory, one launch per sweep, before the levels
-                         above them; 0: default (32 rows, where the subtree launch has at least
-                         152 x 16 warps: measured 5-8 % faster per step at W = 512-1024 on 128x128
-                         arrays, 7 % slower at W = 64 on 64x64 with 500 warps); negative: never */
+  int subtree_rows;   /* level schedule: subtrees at the bottom of the elimination tree spanning at
+                         most this many rows (their columns plus their root's off-diagonal rows,
+                         <= 64) are solved in shared memory in one launch per sweep, before the
+                         levels above them: from 32 problems per warp (W >= 17) one warp per subtree
+                         and 32 problems; below that 32 / WB subtrees of one shape per warp, WB
+                         problems each (W = 1: 32 subtrees, one per lane). 0: default (32 rows, 16
+                         at W = 1; at W >= 17 where the launch has at least 152 x 16 warps, below
+                         where the packs fill at least 152 x 4 warps; measured 5-8 % per step at
+                         W = 512-1024 on 128x128 arrays and at W = 8 on 1024x1024, 4-8 % on W = 1
+                         ragged unions); negative: never */
 } jja_solve_tuning;
 
 /* Builds on the host (no GPU needed) the work-item schedule that jja_plan_create would make for

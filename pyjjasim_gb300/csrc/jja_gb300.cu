@@ -83,8 +83,8 @@ constexpr int kDefaultTargetWarps = 152 * 24;   // levels with fewer work items 
 constexpr int kDefaultMinPiece = 16;     // shortest piece of a split dot product
 constexpr int kDefaultSubRows = 32;     // subtree sweeps: rows per subtree (columns + the root's off-diagonal rows)
 constexpr int kSubMaxRows = 64;          // ... at most this many rows (tuning bound)
-constexpr int kDefaultSubRows1 = 16;     // ... at W = 1 (subtree packs)
-constexpr int kSubPackMinWarps = 152 * 4;   // ... by default at W = 1 from this many warps
+constexpr int kDefaultSubRows1 = 16;     // ... at W = 1 (subtree packs of 32 subtrees)
+constexpr int kSubPackMinWarps = 152 * 4;   // ... where the packs fill at least this many warps
 constexpr int kSubMinWarps = 152 * 16;  // ... by default only when the launch has at least this many warps
 constexpr int kSubMaxWarps = 8;         // ... warps (32-problem blocks of one subtree) per block
 constexpr int kSubMaxK = 8;             // ... members of at most this many columns
@@ -1066,10 +1066,11 @@ __global__ void __launch_bounds__(256) k_subtree(FactorDev F, SubDev S, int W, i
   }
 }
 
-// W = 1 subtree packs: subtrees of one shape (the same members, widths, heights and local row
-// maps; the bottoms of lattices repeat a few hundred shapes) are grouped 32 to a warp, one per
-// lane, with their F values interleaved by lane (the load of a value index is 256 contiguous
-// bytes). Each lane walks its subtree as k_subtree's lanes walk theirs, on its own column of the
+// Subtree packs (below 32 problems per warp): subtrees of one shape (the same members, widths,
+// heights and local row maps; the bottoms of lattices repeat a few hundred shapes) are grouped
+// NS to a warp, NS = 32 / WB slots of WB lanes, one subtree per slot and one problem per lane,
+// with their F values interleaved by slot (the load of a value index is NS contiguous doubles).
+// Each lane walks its subtree for its problem as k_subtree's lanes do, on its own column of the
 // warp's shared buffer; the shape's metadata and row maps are the same for every lane.
 struct SubShape {
   int n, ncols, m_root, f_len;   // members, columns, root rows, F values per subtree
@@ -1078,56 +1079,76 @@ struct SubShape {
 };
 
 struct SubPackDev {
-  const int4* items = nullptr;     // per warp: shape, subtrees (lanes), first lane slot, F values offset / 32
+  const int4* items = nullptr;     // per warp: shape, slots | w0 << 6, first slot, F values offset / NS
   const SubShape* shapes = nullptr;
   const int4* meta = nullptr;      // per member of a shape: column, k, k + m, F offset (in the subtree)
   const int32_t* lrow = nullptr;   // per member of a shape: offset of its row map in the shape's loc
   const uint16_t* loc = nullptr;
-  const int32_t* c0 = nullptr;     // per lane slot: the subtree's first column
-  const int64_t* roff = nullptr;   // per lane slot: its root's rows in F.rows
-  const double* vals = nullptr;    // F values, interleaved by lane
-  int n_items = 0, max_rows = 0;
+  const int32_t* c0 = nullptr;     // per slot: the subtree's first column
+  const int64_t* roff = nullptr;   // per slot: its root's rows in F.rows
+  const double* vals = nullptr;    // F values, interleaved by slot
+  int n_items = 0, max_rows = 0, ns = 0;   // ns: slots per warp (32 / problems per slot)
 };
 
 constexpr int kSubPackWarps = 4;   // warps per block (independent items)
 
-template <bool kForward>
-__global__ void __launch_bounds__(kSubPackWarps * 32) k_subtree_pack(FactorDev F, SubPackDev P, double* __restrict__ b,
-                                                                    double* __restrict__ z, double* __restrict__ x) {
+template <bool kForward, int NS>
+__global__ void __launch_bounds__(kSubPackWarps * 32) k_subtree_pack(FactorDev F, SubPackDev P, int W,
+                                                                    double* __restrict__ b, double* __restrict__ z,
+                                                                    double* __restrict__ x) {
   pdl_begin();
   extern __shared__ double subp_sh[];
+  constexpr int WB = 32 / NS;
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int it = blockIdx.x * kSubPackWarps + wi;
   if (it >= P.n_items) return;
   const int4 item = P.items[it];
-  if (lane >= item.y) return;   // lanes walk independently: no warp-level synchronisation below
+  const int slot = lane / WB, w = (item.y >> 6) + (lane - slot * WB);
+  if (slot >= (item.y & 63) || w >= W) return;   // lanes walk independently: no synchronisation below
   const SubShape T = P.shapes[item.x];
   double* buf = subp_sh + (size_t)wi * P.max_rows * 32 + lane;
-  const int c0 = __ldg(P.c0 + item.z + lane);
-  const int32_t* R = F.rows + __ldg(P.roff + item.z + lane);
-  const double* V = P.vals + (int64_t)item.w * 32 + lane;
+  const int64_t Wl = W;
+  const int64_t c0 = __ldg(P.c0 + item.z + slot);
+  const int32_t* R = F.rows + __ldg(P.roff + item.z + slot);
+  const double* V = P.vals + (int64_t)item.w * NS + slot;
   const uint16_t* loc = P.loc + T.loc_off;
   if (kForward) {
 #pragma unroll 4
-    for (int i = 0; i < T.ncols; ++i) buf[i * 32] = b[c0 + i];
+    for (int i = 0; i < T.ncols; ++i) buf[i * 32] = b[(c0 + i) * Wl + w];
     for (int q = 0; q < T.m_root; ++q) buf[(T.ncols + q) * 32] = 0.0;
     for (int i = 0; i < T.n; ++i) {
       const int4 mt = __ldg(P.meta + T.meta_off + i);
-      sub_member<true, 32>(mt.y, V + (int64_t)mt.w * 32, loc + __ldg(P.lrow + T.meta_off + i), mt.x, mt.z, buf,
-                           z + c0 + mt.x, 1);
+      sub_member<true, NS>(mt.y, V + (int64_t)mt.w * NS, loc + __ldg(P.lrow + T.meta_off + i), mt.x, mt.z, buf,
+                           z + (c0 + mt.x) * Wl + w, Wl);
     }
-    for (int q = 0; q < T.m_root; ++q) atomicAdd(b + __ldg(R + q), buf[(T.ncols + q) * 32]);
+    for (int q = 0; q < T.m_root; ++q) atomicAdd(b + (int64_t)__ldg(R + q) * Wl + w, buf[(T.ncols + q) * 32]);
   } else {
 #pragma unroll 4
-    for (int q = 0; q < T.m_root; ++q) buf[(T.ncols + q) * 32] = __ldcg(x + __ldg(R + q));
+    for (int q = 0; q < T.m_root; ++q) buf[(T.ncols + q) * 32] = __ldcg(x + (int64_t)__ldg(R + q) * Wl + w);
 #pragma unroll 4
-    for (int i = 0; i < T.ncols; ++i) buf[i * 32] = __ldg(z + c0 + i);
+    for (int i = 0; i < T.ncols; ++i) buf[i * 32] = __ldg(z + (c0 + i) * Wl + w);
     for (int i = T.n - 1; i >= 0; --i) {
       const int4 mt = __ldg(P.meta + T.meta_off + i);
-      sub_member<false, 32>(mt.y, V + (int64_t)mt.w * 32, loc + __ldg(P.lrow + T.meta_off + i), mt.x, mt.z, buf,
-                            x + c0 + mt.x, 1);
+      sub_member<false, NS>(mt.y, V + (int64_t)mt.w * NS, loc + __ldg(P.lrow + T.meta_off + i), mt.x, mt.z, buf,
+                            x + (c0 + mt.x) * Wl + w, Wl);
     }
   }
+}
+
+// the pack kernel of a slot count (32, 16, 8, 4 or 2 slots of 1, 2, 4, 8 or 16 problems)
+using SubPackKernel = void (*)(FactorDev, SubPackDev, int, double*, double*, double*);
+SubPackKernel sub_pack_kernel(bool forward, int ns) {
+#define JJA_SUBP(N) \
+  case N: return forward ? k_subtree_pack<true, N> : k_subtree_pack<false, N>;
+  switch (ns) {
+    JJA_SUBP(32)
+    JJA_SUBP(16)
+    JJA_SUBP(8)
+    JJA_SUBP(4)
+    JJA_SUBP(2)
+    default: throw Error(JJA_ERR_INTERNAL, "subtree pack: bad slot count");
+  }
+#undef JJA_SUBP
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1594,15 +1615,15 @@ struct Schedule {
   std::vector<int32_t> sub_lrow;
   std::vector<uint16_t> sub_loc;
   int sub_max_rows = 0, sub_max_f = 0, sub_max_n = 0, sub_max_l = 0;
-  // W = 1: the subtrees grouped by shape into warps (k_subtree_pack; the tables above are then
-  // empty)
+  // below 32 problems per warp: the subtrees grouped by shape into warps (k_subtree_pack; the
+  // tables above are then empty)
   std::vector<int4> sp_items, sp_meta;
   std::vector<SubShape> sp_shapes;
   std::vector<int32_t> sp_lrow, sp_c0;
   std::vector<uint16_t> sp_loc;
   std::vector<int64_t> sp_roff;
   std::vector<double> sp_vals;
-  int sp_max_rows = 0;
+  int sp_max_rows = 0, sp_ns = 0;
 };
 
 // the supernodes a work item covers: one, or the members of a W = 1 pack
@@ -1705,11 +1726,13 @@ void build_subtrees(const jja::Factor& F, int max_rows, Schedule& S, std::vector
   S.n_levels = top + 1;
 }
 
-// W = 1: the subtrees of S (build_subtrees) grouped 32 to a warp by shape: equal member count,
-// columns, root rows, per-member (column, k, k + m, F offset, row-map offset) and row maps, so a
-// warp's lanes run the same walk; their F values (row-major per member) interleaved by lane.
+// Below 32 problems per warp: the subtrees of S (build_subtrees) grouped NS = 32 / WB to a warp by
+// shape: equal member count, columns, root rows, per-member (column, k, k + m, F offset, row-map
+// offset) and row maps, so a warp's lanes run the same walk; their F values (row-major per
+// member) interleaved by slot; one item per pack and block of WB problems in [w_lo, w_hi).
 // Replaces S's per-subtree tables.
-void build_subtree_packs(const jja::Factor& F, Schedule& S) {
+void build_subtree_packs(const jja::Factor& F, Schedule& S, int WB, int w_lo, int w_hi) {
+  const int NS = 32 / WB;
   std::map<std::vector<int>, std::vector<int>> by_shape;
   for (int t = 0; t < (int)S.subs.size(); ++t) {
     const SubTree& T = S.subs[t];
@@ -1739,13 +1762,13 @@ void build_subtree_packs(const jja::Factor& F, Schedule& S) {
     const int shape = (int)S.sp_shapes.size();
     S.sp_shapes.push_back(sh);
     S.sp_max_rows = std::max(S.sp_max_rows, sh.ncols + sh.m_root);
-    for (size_t i = 0; i < ts.size(); i += 32) {
-      const int count = (int)std::min<size_t>(32, ts.size() - i);
-      const int64_t lane0 = (int64_t)S.sp_c0.size(), off = (int64_t)S.sp_vals.size() / 32;
+    for (size_t i = 0; i < ts.size(); i += NS) {
+      const int count = (int)std::min<size_t>(NS, ts.size() - i);
+      const int64_t lane0 = (int64_t)S.sp_c0.size(), off = (int64_t)S.sp_vals.size() / NS;
       if (lane0 >= INT32_MAX || off >= INT32_MAX) throw Error(JJA_ERR_ARG, "too many subtree packs");
-      S.sp_vals.resize(S.sp_vals.size() + (size_t)32 * sh.f_len, 0.0);
-      double* vals = S.sp_vals.data() + off * 32;
-      for (int l = 0; l < 32; ++l) {
+      S.sp_vals.resize(S.sp_vals.size() + (size_t)NS * sh.f_len, 0.0);
+      double* vals = S.sp_vals.data() + off * NS;
+      for (int l = 0; l < NS; ++l) {
         if (l >= count) {
           S.sp_c0.push_back(0);
           S.sp_roff.push_back(0);
@@ -1760,12 +1783,16 @@ void build_subtree_packs(const jja::Factor& F, Schedule& S) {
           const double* src = F.fcol.data() + F.sn_valptr[u];
           const int64_t f = F.sn_valptr[u] - T.f_off;
           for (int r = 0; r < nf; ++r)
-            for (int j = 0; j < k; ++j) vals[(f + (int64_t)r * k + j) * 32 + l] = src[(int64_t)j * nf + r];
+            for (int j = 0; j < k; ++j) vals[(f + (int64_t)r * k + j) * NS + l] = src[(int64_t)j * nf + r];
         }
       }
-      S.sp_items.push_back(make_int4(shape, count, (int)lane0, (int)off));
+      for (int w0 = w_lo; w0 < w_hi; w0 += WB) {
+        if (w0 >= (1 << 25)) throw Error(JJA_ERR_ARG, "subtree packs: too many problems");
+        S.sp_items.push_back(make_int4(shape, count | (w0 << 6), (int)lane0, (int)off));
+      }
     }
   }
+  S.sp_ns = NS;
   S.subs.clear();
   S.sub_meta.clear();
   S.sub_lrow.clear();
@@ -1812,7 +1839,7 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
   }
   // subtree sweeps at the bottom of the tree (level schedule, 32 problems per warp); the other
   // supernodes are re-levelled above them
-  const int sub_rows = ((WB == 32 || W == 1) && tu.schedule <= 1 && tu.subtree_rows >= 0)
+  const int sub_rows = (tu.schedule <= 1 && tu.subtree_rows >= 0)
                            ? (tu.subtree_rows ? tu.subtree_rows : (W == 1 ? kDefaultSubRows1 : kDefaultSubRows)) : 0;
   std::vector<int> level(F.sn_level.begin(), F.sn_level.end());
   std::vector<char> inside(F.ns, 0);
@@ -1820,7 +1847,7 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
     build_subtrees(F, sub_rows, S, inside, level);
     // by default only where the subtree launch has warps enough to hide each warp's walk (a
     // subtree is walked member by member; the levels it replaces run its rows in parallel)
-    if (W > 1 && !tu.subtree_rows && (int64_t)S.subs.size() * ((W + 31) / 32) < kSubMinWarps) {
+    if (WB == 32 && !tu.subtree_rows && (int64_t)S.subs.size() * ((W + 31) / 32) < kSubMinWarps) {
       S.subs.clear();
       S.sub_meta.clear();
       S.sub_lrow.clear();
@@ -1830,8 +1857,8 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
       level.assign(F.sn_level.begin(), F.sn_level.end());
       inside.assign(F.ns, 0);
     }
-    if (W == 1) {
-      build_subtree_packs(F, S);
+    if (WB < 32) {
+      build_subtree_packs(F, S, WB, w_lo, w_hi);
       // by default only where the packs fill warps enough (a few hundred subtree packs walk
       // slower than the levels they replace)
       if (!tu.subtree_rows && (int64_t)S.sp_items.size() < kSubPackMinWarps) {
@@ -2311,8 +2338,8 @@ void launch_subtrees(jja_plan* p, const Group& g, cudaStream_t st, bool forward,
   if (p->subp.n_items) {
     const int grid = (p->subp.n_items + kSubPackWarps - 1) / kSubPackWarps;
     const size_t smem = (size_t)kSubPackWarps * p->subp.max_rows * 32 * sizeof(double);
-    launch_smem(p->pdl, forward ? k_subtree_pack<true> : k_subtree_pack<false>, dim3((unsigned)grid),
-                kSubPackWarps * 32, smem, st, p->F, p->subp, b, z, x);
+    launch_smem(p->pdl, sub_pack_kernel(forward, p->subp.ns), dim3((unsigned)grid), kSubPackWarps * 32, smem, st,
+                p->F, p->subp, p->W, b, z, x);
   }
   if (!p->sub.n) return;
   const int blocks = (g.wn + 31) / 32;
@@ -2753,10 +2780,12 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
       sp.vals = p->up(S.sp_vals.data(), S.sp_vals.size());
       sp.n_items = (int)S.sp_items.size();
       sp.max_rows = S.sp_max_rows;
+      sp.ns = S.sp_ns;
       // the attribute is the kernel's, shared by every plan: the largest any plan can need
       const int smem = (int)((size_t)kSubPackWarps * kSubMaxRows * 32 * sizeof(double));
-      JJA_CUDA(cudaFuncSetAttribute(k_subtree_pack<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-      JJA_CUDA(cudaFuncSetAttribute(k_subtree_pack<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      for (int fw = 0; fw < 2; ++fw)
+        JJA_CUDA(cudaFuncSetAttribute(sub_pack_kernel(fw != 0, sp.ns), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      smem));
     }
     if (!S.subs.empty()) {
       SubDev& sd = p->sub;

@@ -31,8 +31,8 @@ def test_schedule_with_subtrees(lattice, n, ordering):
     for rows in (8, 32, 64):
         n_on = f.check_schedule(64, {"subtree_rows": rows})
         assert n_on[0] < n_off[0] and n_on[1] <= n_off[1]
-    # below 32 problems per warp no subtrees are built
-    assert f.check_schedule(8, {"subtree_rows": 32}) == f.check_schedule(8, {"subtree_rows": -1})
+    # below 32 problems per warp the subtrees go into packs of one shape (fewer level items)
+    assert f.check_schedule(8, {"subtree_rows": 32})[0] < f.check_schedule(8, {"subtree_rows": -1})[0]
 
 
 def test_default_takes_subtrees_where_the_launch_is_wide():
@@ -64,6 +64,28 @@ def test_subtree_solve_matches_scipy(lattice, n, W, ordering, rows):
     A, K = P.face_matrix(c, 0.05)
     b = _rhs(K, W, n + W + rows)
     x = backend.solve_faces(c, 0.05, b, ordering=ordering, tuning={"subtree_rows": rows})
+    ref = scipy.sparse.linalg.spsolve(K.tocsc(), b).reshape(x.shape)
+    assert float(np.abs(x - ref).max()) <= 1e-11 * float(np.abs(ref).max())
+
+
+@pytest.mark.parametrize("W", [2, 3, 8, 16])
+def test_small_w_schedule_packs_subtrees_by_shape(W):
+    # below 32 problems per warp: subtrees of one shape share a warp, 32 / WB of them
+    f = _factor(SquareArray(96, 96), W, "nd")
+    n_off = f.check_schedule(W, {"subtree_rows": -1})
+    n_on = f.check_schedule(W, {"subtree_rows": 16})
+    assert n_on[0] < n_off[0] and n_on[1] < n_off[1]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("W", [2, 3, 8, 16])
+@pytest.mark.parametrize("lattice,n,ordering", [("square", 96, "nd"), ("honeycomb", 40, "mmd")])
+def test_small_w_subtree_packs_solve_matches_scipy(lattice, n, ordering, W):
+    c = LATTICES[lattice](n, n)
+    c.set_inductance(0.03)
+    A, K = P.face_matrix(c, 0.05)
+    b = _rhs(K, W, n + W)
+    x = backend.solve_faces(c, 0.05, b, ordering=ordering, tuning={"subtree_rows": 16})
     ref = scipy.sparse.linalg.spsolve(K.tocsc(), b).reshape(x.shape)
     assert float(np.abs(x - ref).max()) <= 1e-11 * float(np.abs(ref).max())
 
