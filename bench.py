@@ -814,7 +814,8 @@ def main():
             traffic = None
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
         line["roofline"] = {
-            "kernel": "forward supernodal solve (k_fwd_level, all levels of one step)",
+            "kernel": "forward supernodal solve (k_subtree<fwd> for the bottom subtrees + k_fwd_level for the "
+                      "levels above, one step, all problem groups)",
             "bound": "fp64", "achieved": fwd_flops / fwd_s / 1e12, "peak": fp64, "unit": "TFLOP/s",
             "frac": (fwd_flops / fwd_s / 1e12) / fp64,
             "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (FP64 has no entry in MEASURED_PEAKS.json)",

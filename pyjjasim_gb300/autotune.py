@@ -21,8 +21,9 @@ GPU depends on choices that have no single best value across array sizes and bat
   lanes take more rows);
 * ``target_warps``: how aggressively the few, long dot products at the top of the elimination
   tree are split into atomically accumulated pieces;
-* ``subtree_rows``: from 32 problems per warp, how large the subtrees at the bottom of the tree
-  are that one warp solves in shared memory (0: the library's rule; -1: none).
+* ``subtree_rows``: how large the subtrees at the bottom of the tree are that are solved in
+  shared memory in one launch per sweep (one warp per subtree from 32 problems per warp, packs of
+  subtrees of one shape below; 0: the library's rule; -1: none).
 
 ``autotune`` times candidates with CUDA events on graph-replayed steps of a synthetic problem
 on the same circuit, time step, stencil width and W (the step's cost does not depend on the
@@ -74,7 +75,7 @@ def candidates(W):
         "rows_per_lane_fwd": [0, 1, 2, 4],
         "rhs_block": [0] + [b for b in (wb // 2, wb // 4) if b >= 1],
         "target_warps": [152 * 24, 152 * 8, 152 * 64],
-        "subtree_rows": [0, -1, 24, 48] if W >= 17 else [0],
+        "subtree_rows": [0, -1, 24, 48] if W >= 17 else [0, -1, 16, 32],
         "relax": [(-1, -1.0), (0, 0.0), (64, 0.1)],
     }
 
