@@ -114,3 +114,26 @@ def test_vortex_flow_gradient_matches_finite_differences():
         fd = (flow(*plus) - flow(*minus)) / (2 * h)
         scale = np.abs(fd).max() + 1e-12
         assert np.abs(ad - fd).max() <= 1e-5 * scale + 1e-9, f"{name}: adjoint {ad} vs finite differences {fd}"
+
+
+@pytest.mark.parametrize("W_s,tuning", [(32, {"subtree_rows": 32}), (8, {"subtree_rows": 32})])
+def test_adjoint_with_subtree_sweeps_matches_level_sweeps(W_s, tuning):
+    """The adjoint's face solves run through the same sweep schedule as the forward steps: with
+    the bottom subtrees solved in shared memory (one warp per subtree and 32 problems, or packs
+    of subtrees of one shape below 32 problems) the gradients equal those of the level-only
+    schedule up to summation order."""
+    rng = np.random.default_rng(5)
+    c = SquareArray(24, 24)
+    Nj, Nf = c.junction_count(), c.face_count()
+    Ic = rng.lognormal(0.0, 0.2, (Nj, W_s))
+    Is = c.current_base(0.0)[:, None, None] * np.linspace(1.1, 1.5, W_s)[None, :, None]
+    prob = TimeEvolutionProblem(c, time_step=0.05, time_step_count=160, current_sources=Is, external_flux=0.12,
+                                store_time_steps=[79, 159], store_voltage=False, store_current=False)
+    weights = time_averaged_voltage_weights(prob, 79, 159, np.arange(24 * 23))
+    grads = []
+    for t in (tuning, {"subtree_rows": -1}):
+        run = AdjointRun(prob, weights, Ic=Ic, ordering="nd", tuning=t)
+        grads.append({k: v.cpu().numpy() for k, v in run.backward().items()})
+    for k in grads[0]:
+        a, b = grads[0][k], grads[1][k]
+        assert np.abs(a - b).max() <= 1e-9 * max(1.0, np.abs(b).max()), k
