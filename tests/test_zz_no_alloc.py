@@ -8,7 +8,9 @@ checks each result against jja_solve's (the allocating entry point) within the 1
 tolerance the face-solve tests use; the two calls also show that the array's leftover contents
 from one call do not leak into the next. It covers both schedules of the triangular sweeps
 (one launch per level, and the dataflow sweep whose bounded waits are confirmed by the plan
-check after every call) and one problem per launch with small supernodes solved one per lane.
+check after every call), one problem per launch with small supernodes solved one per lane, and
+the subtree sweeps (one warp per subtree and 32 problems, and packs of subtrees of one shape for
+8 problems and for one).
 """
 import ctypes
 
@@ -30,7 +32,9 @@ def _plan(n, W, tuning=None):
 
 
 @pytest.mark.parametrize("W,tuning", [(24, {"schedule": 1}), (24, {"schedule": 2}),
-                                      (1, {"pack_min_warps": 1}), (1, {"schedule": 2})])
+                                      (1, {"pack_min_warps": 1}), (1, {"schedule": 2}),
+                                      (24, {"subtree_rows": 32}), (8, {"subtree_rows": 32}),
+                                      (1, {"subtree_rows": 16})])
 def test_static_solve_matches_allocating_solve_twice(W, tuning):
     import torch
     lib = N.lib()
