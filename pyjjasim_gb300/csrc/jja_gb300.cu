@@ -1360,6 +1360,45 @@ __device__ __forceinline__ void dst_pair(double2* a, const double* x1, const dou
   }
 }
 
+// One line per transform, at half the length: the odd extension e of x (n = 2N values, N = m + 1,
+// real) packed as z_p = e_{2p} + i e_{2p+1}, p < N, loaded in bit-reversed order and transformed
+// in place by an N-point FFT (twiddles W_N^q = W_n^{2q}); dst_line_out then forms the n-point
+// transform of e from Z_k and Z_{N-k}. Half the butterflies of the n-point transform, one line
+// per block (all SMs busy where pairing two lines would halve the blocks).
+__device__ __forceinline__ void dst_line(double2* a, const double* x, int64_t stride, int m, int lg,
+                                         const double2* tw) {
+  const int N = m + 1, n = 2 * N, lgN = lg - 1;
+  auto ext = [&](int j) -> double {   // e_j
+    if (j >= 1 && j <= m) return x[(int64_t)(j - 1) * stride];
+    if (j > N) return -x[(int64_t)(n - j - 1) * stride];
+    return 0.0;
+  };
+  for (int p = threadIdx.x; p < N; p += blockDim.x)
+    a[__brev((unsigned)p) >> (32 - lgN)] = make_double2(ext(2 * p), ext(2 * p + 1));
+  __syncthreads();
+  for (int l = 1; l <= lgN; ++l) {
+    const int half = 1 << (l - 1), tstride = (N >> l) * 2;
+    for (int j = threadIdx.x; j < N / 2; j += blockDim.x) {
+      const int pos = j & (half - 1);
+      const int i0 = ((j >> (l - 1)) << l) + pos, i1 = i0 + half;
+      const double2 w = tw[pos * tstride];
+      const double2 u = a[i0], v = a[i1];
+      const double2 t = make_double2(fma(w.x, v.x, -w.y * v.y), fma(w.x, v.y, w.y * v.x));
+      a[i0] = make_double2(u.x + t.x, u.y + t.y);
+      a[i1] = make_double2(u.x - t.x, u.y - t.y);
+    }
+    __syncthreads();
+  }
+}
+
+// the line's DST-I value at k = 1..m: with A = Z_k, B = conj Z_{N-k}, the n-point transform is
+// E_k = (A + B) / 2 - (i / 2) W_n^k (A - B), and the DST-I sum is -Im(E_k) / 2
+__device__ __forceinline__ double dst_line_out(const double2* a, int N, int k, const double2* tw) {
+  const double2 A = a[k], Bc = a[N - k], w = tw[k];
+  const double re = fma(w.x, A.x - Bc.x, -w.y * (A.y + Bc.y));   // Re(W^k (A - B))
+  return 0.25 * (re - (A.y - Bc.y));
+}
+
 // the twiddles of a transform into shared memory (visible after the caller's next barrier)
 __device__ __forceinline__ void load_twiddles(double2* dst, const double2* __restrict__ src, int count) {
   for (int i = threadIdx.x; i < count; i += blockDim.x) dst[i] = __ldg(src + i);
@@ -1396,9 +1435,11 @@ __global__ void k_dst_rows(DstArgs d, const double* in, double* out, int W, int 
     src0 = in + ((int64_t)w * d.my + iy0) * d.mx;
     if (two) src1 = src0 + d.mx;
   }
-  dst_pair(fft_buf, src0, src1, 1, d.mx, d.lgx, tws);
+  if (two) dst_pair(fft_buf, src0, src1, 1, d.mx, d.lgx, tws);
+  else dst_line(fft_buf, src0, 1, d.mx, d.lgx, tws);
   for (int k = threadIdx.x; k < d.mx; k += blockDim.x) {
-    const double2 y = dst_pair_out(fft_buf, n, k + 1);
+    const double2 y = two ? dst_pair_out(fft_buf, n, k + 1)
+                          : make_double2(dst_line_out(fft_buf, d.mx + 1, k + 1, tws), 0.0);
     if (out_faces) {
       out[(int64_t)__ldg(d.grid_face + iy0 * d.mx + k) * W + w] = y.x;
       if (two) out[(int64_t)__ldg(d.grid_face + iy1 * d.mx + k) * W + w] = y.y;
@@ -1419,19 +1460,23 @@ __global__ void k_dst_cols(DstArgs d, int w0, int lines) {
   double* tmp = reinterpret_cast<double*>(fft_buf + n);   // 2 x my values after the FFT buffer
   double2* tws = fft_buf + n + d.my;                      // then the twiddles
   load_twiddles(tws, d.twy, n / 2);
-  dst_pair(fft_buf, col, two ? col + 1 : nullptr, d.mx, d.my, d.lgy, tws);
+  if (two) dst_pair(fft_buf, col, col + 1, d.mx, d.my, d.lgy, tws);
+  else dst_line(fft_buf, col, d.mx, d.my, d.lgy, tws);
   const double lx0 = __ldg(d.lamx + kx0), lx1 = two ? __ldg(d.lamx + kx1) : 0.0;
   for (int k = threadIdx.x; k < d.my; k += blockDim.x) {
-    const double2 y = dst_pair_out(fft_buf, n, k + 1);
+    const double2 y = two ? dst_pair_out(fft_buf, n, k + 1)
+                          : make_double2(dst_line_out(fft_buf, d.my + 1, k + 1, tws), 0.0);
     const double ly = __ldg(d.lamy + k);
     tmp[k] = y.x * d.scale / (lx0 + ly);
     tmp[d.my + k] = two ? y.y * d.scale / (lx1 + ly) : 0.0;
   }
   __syncthreads();
-  dst_pair(fft_buf, tmp, two ? tmp + d.my : nullptr, 1, d.my, d.lgy, tws);
+  if (two) dst_pair(fft_buf, tmp, tmp + d.my, 1, d.my, d.lgy, tws);
+  else dst_line(fft_buf, tmp, 1, d.my, d.lgy, tws);
   double* out = d.t2 + (int64_t)w * d.my * d.mx + kx0;
   for (int k = threadIdx.x; k < d.my; k += blockDim.x) {
-    const double2 y = dst_pair_out(fft_buf, n, k + 1);
+    const double2 y = two ? dst_pair_out(fft_buf, n, k + 1)
+                          : make_double2(dst_line_out(fft_buf, d.my + 1, k + 1, tws), 0.0);
     out[(int64_t)k * d.mx] = y.x;
     if (two) out[(int64_t)k * d.mx + 1] = y.y;
   }
