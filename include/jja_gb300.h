@@ -132,6 +132,19 @@ typedef struct {
 int jja_factor_check_schedule(const jja_factor* f, int W, const jja_solve_tuning* tuning, int64_t* n_fwd_items,
                               int64_t* n_bwd_items);
 
+/* Shape of that schedule (host only, no GPU needed). */
+typedef struct {
+  int n_levels;            /* level launches per sweep (above the subtrees) */
+  int n_subtrees;          /* bottom subtrees solved in shared memory (0: none) */
+  int n_subtree_members;   /* supernodes inside them (they have no level items) */
+  int max_subtree_rows;    /* largest subtree: columns plus its root's off-diagonal rows */
+  int n_pack_items;        /* below 32 problems per warp: warps of subtree packs */
+  int n_pack_shapes;       /* ... distinct subtree shapes among them */
+  int64_t n_fwd_items;     /* level work items of the forward sweep */
+  int64_t n_bwd_items;     /* ... of the backward sweep */
+} jja_schedule_stats;
+int jja_factor_schedule_stats(const jja_factor* f, int W, const jja_solve_tuning* tuning, jja_schedule_stats* out);
+
 typedef struct {
   int Nj, Nf, W;           /* junctions, faces, problems per launch */
   int stencil_width;       /* 3, 4 or 5 (time_evolution.py:401-408) */

@@ -36,6 +36,11 @@ class SolveTuning(ctypes.Structure):
                 ("subtree_rows", c_int)]
 
 
+class ScheduleStats(ctypes.Structure):
+    _fields_ = [("n_levels", c_int), ("n_subtrees", c_int), ("n_subtree_members", c_int), ("max_subtree_rows", c_int),
+                ("n_pack_items", c_int), ("n_pack_shapes", c_int), ("n_fwd_items", c_int64), ("n_bwd_items", c_int64)]
+
+
 class PlanDesc(ctypes.Structure):
     _fields_ = [("Nj", c_int), ("Nf", c_int), ("W", c_int), ("stencil_width", c_int),
                 ("a_rowptr", P_i64), ("a_col", P_i32), ("a_val", P_f64),
@@ -95,6 +100,7 @@ SIGNATURES = {
     "jja_factor_get_supernodes": (c_int, [c_void_p, P_i32, P_i32, P_i32, P_i32, P_i32]),
     "jja_factor_solve_host": (c_int, [c_void_p, P_f64, c_int]),
     "jja_factor_check_schedule": (c_int, [c_void_p, c_int, ctypes.POINTER(SolveTuning), P_i64, P_i64]),
+    "jja_factor_schedule_stats": (c_int, [c_void_p, c_int, ctypes.POINTER(SolveTuning), ctypes.POINTER(ScheduleStats)]),
     "jja_plan_create": (c_int, [ctypes.POINTER(PlanDesc), c_void_p, ctypes.POINTER(c_void_p)]),
     "jja_plan_destroy": (None, [c_void_p]),
     "jja_plan_device_bytes": (c_int64, [c_void_p]),

@@ -1660,6 +1660,7 @@ struct Schedule {
   std::vector<int32_t> sub_lrow;
   std::vector<uint16_t> sub_loc;
   int sub_max_rows = 0, sub_max_f = 0, sub_max_n = 0, sub_max_l = 0;
+  int sub_total = 0, sub_members = 0, sub_rows_max = 0;   // kept when the tables become packs
   // below 32 problems per warp: the subtrees grouped by shape into warps (k_subtree_pack; the
   // tables above are then empty)
   std::vector<int4> sp_items, sp_meta;
@@ -1754,11 +1755,14 @@ void build_subtrees(const jja::Factor& F, int max_rows, Schedule& S, std::vector
       }
     }
     S.sub_max_rows = std::max(S.sub_max_rows, T.ncols + T.m_root);
+    S.sub_rows_max = S.sub_max_rows;
+    S.sub_members += T.n;
     S.sub_max_f = std::max(S.sub_max_f, (T.f_len + 1) / 2 * 2);
     S.sub_max_n = std::max(S.sub_max_n, T.n);
     S.sub_max_l = std::max(S.sub_max_l, T.l_len);
     S.subs.push_back(T);
   }
+  S.sub_total = (int)S.subs.size();
   // the remaining supernodes: leaves (or parents of subtrees only) at level 0
   int top = -1;
   for (int s = 0; s < ns; ++s) if (!inside[s]) level[s] = 0;
@@ -1898,6 +1902,7 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
       S.sub_lrow.clear();
       S.sub_loc.clear();
       S.sub_max_rows = S.sub_max_f = S.sub_max_n = S.sub_max_l = 0;
+      S.sub_total = S.sub_members = S.sub_rows_max = 0;
       S.n_levels = F.n_levels;
       level.assign(F.sn_level.begin(), F.sn_level.end());
       inside.assign(F.ns, 0);
@@ -2714,6 +2719,25 @@ int jja_factor_check_schedule(const jja_factor* f, int W, const jja_solve_tuning
     check_schedule(S);
     if (n_fwd_items) *n_fwd_items = (int64_t)S.fi.size();
     if (n_bwd_items) *n_bwd_items = (int64_t)S.bi_flow.size();
+  });
+}
+
+int jja_factor_schedule_stats(const jja_factor* f, int W, const jja_solve_tuning* tuning, jja_schedule_stats* out) {
+  return guarded([&] {
+    if (!f || !out) throw Error(JJA_ERR_ARG, "jja_factor_schedule_stats: null argument");
+    jja_solve_tuning tu{};
+    if (tuning) tu = *tuning;
+    const Schedule S = build_schedule(*f->f, W, tu);
+    jja_schedule_stats st{};
+    st.n_levels = S.n_levels;
+    st.n_subtrees = S.sub_total;
+    st.n_subtree_members = S.sub_members;
+    st.max_subtree_rows = S.sub_rows_max;
+    st.n_pack_items = (int)S.sp_items.size();
+    st.n_pack_shapes = (int)S.sp_shapes.size();
+    st.n_fwd_items = (int64_t)S.fi.size();
+    st.n_bwd_items = (int64_t)S.bi.size();
+    *out = st;
   });
 }
 

@@ -114,6 +114,15 @@ class HostFactor:
                                                   ctypes.byref(nb)))
         return nf.value, nb.value
 
+    def schedule_stats(self, W, tuning=None):
+        """dict: the shape of the GPU schedule for W problems (levels, bottom subtrees, subtree
+        packs, work items), built on the host as the plan builds it."""
+        t = dict(tuning or {})
+        tu = N.SolveTuning(*(int(t.get(f, 0)) for f in TUNING_FIELDS))
+        st = N.ScheduleStats()
+        N.check(N.lib().jja_factor_schedule_stats(self.handle, int(W), ctypes.byref(tu), ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in N.ScheduleStats._fields_}
+
     def solve_host(self, b):
         """Host solve (diagnostic). b: (n,) or (n, nrhs)."""
         b = np.array(b, dtype=np.float64, order="C", copy=True)

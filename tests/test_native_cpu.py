@@ -187,5 +187,5 @@ def test_ctypes_structs_match_the_header():
     for cname, pystruct in (("jja_solve_tuning", N.SolveTuning), ("jja_view", N.View), ("jja_state", N.State),
                             ("jja_plan_desc", N.PlanDesc), ("jja_adjoint_args", N.AdjointArgs),
                             ("jja_adjoint_segment_args", N.AdjointSegmentArgs), ("jja_factor_opts", N.FactorOpts),
-                            ("jja_factor_stats", N.FactorStats)):
+                            ("jja_factor_stats", N.FactorStats), ("jja_schedule_stats", N.ScheduleStats)):
         assert c_fields(cname) == [f for f, _ in pystruct._fields_], cname

@@ -144,3 +144,50 @@ def test_trajectories_with_and_without_subtrees_agree():
     th_off, _ = backend.time_evolution_core(prob, mask, mask, tuning={"subtree_rows": -1})
     scale = max(1.0, float(np.abs(th_off).max()))
     assert float(np.abs(th_on - th_off).max()) <= 1e-11 * scale
+
+
+def _python_subtrees(f, max_rows):
+    """The subtree selection restated from the factor's supernode table: a supernode qualifies
+    when its subtree's columns plus its own off-diagonal rows are at most max_rows, no member is
+    wider than 8 columns, and the staged F values and row maps stay within 2048 and 4096 entries;
+    the subtrees are the qualifying supernodes whose parent does not qualify. The others are
+    re-levelled: level 0 when no child remains outside a subtree, else 1 + the largest child level."""
+    sn = f.supernodes()
+    k, m, par = sn["k"].astype(np.int64), sn["m"].astype(np.int64), sn["parent"]
+    ns = len(k)
+    cols, fl, ll, kmax, cnt = k.copy(), (k + m) * k, m.copy(), k.copy(), np.ones(ns, np.int64)
+    for s in range(ns):
+        p = par[s]
+        if p >= 0:
+            cols[p] += cols[s]; fl[p] += fl[s]; ll[p] += ll[s]; kmax[p] = max(kmax[p], kmax[s]); cnt[p] += cnt[s]
+    ok = (cols + m <= max_rows) & (kmax <= 8) & (fl <= 2048) & (ll <= 4096)
+    roots = [s for s in range(ns) if ok[s] and (par[s] < 0 or not ok[par[s]])]
+    level = np.zeros(ns, np.int64)
+    top = -1
+    for s in range(ns):
+        if ok[s]:
+            continue
+        top = max(top, level[s])
+        if par[s] >= 0:
+            level[par[s]] = max(level[par[s]], level[s] + 1)
+    return len(roots), int(ok.sum()), int(max((cols + m)[roots], default=0)), top + 1
+
+
+@pytest.mark.parametrize("lattice,n,ordering,W,rows", [("square", 128, "mmd", 512, 32), ("square", 64, "nd", 64, 24),
+                                                       ("honeycomb", 40, "nd", 32, 48), ("triangular", 48, "mmd", 8, 32),
+                                                       ("square", 96, "nd", 1, 16)])
+def test_schedule_stats_match_the_subtree_rule(lattice, n, ordering, W, rows):
+    f = _factor(LATTICES[lattice](n, n), W, ordering)
+    st = f.schedule_stats(W, {"subtree_rows": rows})
+    n_sub, members, max_rows, levels = _python_subtrees(f, rows)
+    assert (st["n_subtrees"], st["n_subtree_members"], st["max_subtree_rows"], st["n_levels"]) == \
+        (n_sub, members, max_rows, levels)
+    if W < 32:      # packs of 32 / WB subtrees of one shape, one item per pack and problem block
+        wb = 1 << max(0, (W - 1).bit_length())
+        assert st["n_pack_shapes"] <= n_sub
+        assert st["n_pack_items"] >= -(-n_sub // (32 // wb)) * (-(-W // wb))
+    else:
+        assert st["n_pack_items"] == 0
+    off = f.schedule_stats(W, {"subtree_rows": -1})
+    assert off["n_subtrees"] == 0 and off["n_levels"] == f.stats["n_levels"]
+    assert (st["n_fwd_items"], st["n_bwd_items"]) == f.check_schedule(W, {"subtree_rows": rows})
