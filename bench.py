@@ -389,20 +389,25 @@ def ragged_leg(G, torch, n_problems, steps, bases):
     main = torch.cuda.current_stream()
     RaggedBatch.run_simulations(sims, 16 * (sims[0].width - 1) + 1)
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(main)
-    for sim in sims:
-        sim.stream.wait_event(e0)
-    RaggedBatch.run_simulations(sims, steps)
-    for sim in sims:
-        done = torch.cuda.Event()
-        done.record(sim.stream)
-        main.wait_event(done)
-    e1.record(main)
-    e1.synchronize()
-    for sim in sims:
-        sim.synchronize()
-    el = e0.elapsed_time(e1) / 1e3
+
+    def timed_run():
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(main)
+        for sim in sims:
+            sim.stream.wait_event(e0)
+        RaggedBatch.run_simulations(sims, steps)
+        for sim in sims:
+            done = torch.cuda.Event()
+            done.record(sim.stream)
+            main.wait_event(done)
+        e1.record(main)
+        e1.synchronize()
+        for sim in sims:
+            sim.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    runs = [timed_run() for _ in range(2)]   # best of two: the parts' host threads share the machine's cores
+    el = min(runs)
     from collections import Counter
     kinds_used = Counter(["square", "honeycomb", "triangular"][int(k)] for k in kinds[:n_problems])
     return {"workload": f"ragged: {n_problems} of 256 seeded problems (square/honeycomb/triangular, side "
@@ -410,6 +415,8 @@ def ragged_leg(G, torch, n_problems, steps, bases):
                         f"systems ({len(sims)} parts stepped concurrently)",
             "problems": n_problems, "parts": len(sims), "Nj_total": rb.Nj, "Nf_total": rb.Nf, "steps": steps,
             "ms_per_step": el / steps * 1e3, "value": rb.Nj * steps / el, "unit": "junction-steps/s",
+            "ms_per_step_runs": [r / steps * 1e3 for r in runs],
+            "timing": f"CUDA events around {steps} graph-replayed steps of all parts, best of two runs",
             "setup_seconds": t_setup,
             "setup_breakdown_seconds": {"problems": t_problems, "unions": t_union,
                                         "factor_and_plans": t_setup - t_problems - t_union},
