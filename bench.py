@@ -186,8 +186,11 @@ def adjoint_leg(G, torch, Nt):
 
 
 def _timed_steps(torch, sim, steps):
-    """Device seconds of `steps` graph-replayed steps (after one graph's warm-up)."""
-    sim.run(16 * (sim.width - 1) + 1, use_graph=True)
+    """Device seconds of `steps` graph-replayed steps. The warm-up of 32 history-rotation periods
+    captures the graphs of every length (32, 16, 8, 4 and 2 periods) for the rotation phase the
+    timed run starts in (graphs are keyed by the history buffers), so no capture falls inside the
+    timed region."""
+    sim.run(32 * (sim.width - 1), use_graph=True)
     sim.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(sim.stream)
@@ -387,7 +390,7 @@ def ragged_leg(G, torch, n_problems, steps, bases):
     # the parts step concurrently on their own streams (one host thread each): fork from and
     # join into one timing stream
     main = torch.cuda.current_stream()
-    RaggedBatch.run_simulations(sims, 16 * (sims[0].width - 1) + 1)
+    RaggedBatch.run_simulations(sims, 32 * (sims[0].width - 1))   # every graph length, as _timed_steps
     torch.cuda.synchronize()
 
     def timed_run():
