@@ -34,6 +34,17 @@ def test_candidates_respect_the_batch_width():
     assert AT.candidates(1)["rhs_block"] == [0]          # one problem: one lane per problem only
     assert AT.candidates(8)["rhs_block"] == [0, 4, 2]
     assert AT.candidates(512)["rhs_block"] == [0, 16, 8]
+    # subtree sizes: the library's rule first, none, then sizes that fit the subtree kernels
+    for W in (1, 8, 17, 512):
+        cand = AT.candidates(W)["subtree_rows"]
+        assert cand[0] == 0 and -1 in cand and all(r <= 64 for r in cand)
+
+
+def test_tuned_options_carry_every_solve_field():
+    opts = AT.to_options(dict(AT.DEFAULT, subtree_rows=24, groups=3))
+    assert opts["tuning"]["subtree_rows"] == 24 and opts["tuning"]["groups"] == 3
+    from pyjjasim_gb300 import plan as P
+    assert set(opts["tuning"]) <= set(P.TUNING_FIELDS)
 
 
 def test_cache_is_written_and_reused(tmp_path, monkeypatch):
@@ -69,7 +80,9 @@ def test_cache_is_written_and_reused(tmp_path, monkeypatch):
                                             "target_warps": 152 * 200}, (64, 0.1)),
                                           ({"pdl": 1}, (-1, -1.0)),
                                           ({"groups": 1}, (-1, -1.0)),
-                                          ({"pdl": 1, "schedule": 2, "rows_per_lane": 4}, (0, 0.0))])
+                                          ({"pdl": 1, "schedule": 2, "rows_per_lane": 4}, (0, 0.0)),
+                                          ({"subtree_rows": 24}, (-1, -1.0)), ({"subtree_rows": 64}, (0, 0.0)),
+                                          ({"subtree_rows": 16, "rhs_block": 4}, (-1, -1.0))])
 def test_tuned_launch_shapes_agree_with_default(tuning, relax):
     from pyjjasim_gb300 import TimeEvolutionProblem, backend
     c = SquareArray(20, 23)
