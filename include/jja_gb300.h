@@ -84,14 +84,15 @@ typedef struct {
   int rhs_block;      /* problems per warp: a power of two <= 32 (default min(W, 32) rounded up) */
   int rows_per_lane;  /* output rows per lane of a work item: 1, 2, 4 or 8 (default 1) */
   int target_warps;   /* levels with fewer work items split their dot products until they have
-                         this many (default 152 x 24) */
+                         this many (default 152 x 24; 152 x 64 for 2-16 problems) */
   int min_piece;      /* shortest piece of a split dot product (default 16) */
   int schedule;       /* 1: one launch per elimination-tree level; 2: dataflow, one persistent
                          launch per sweep whose work items wait (bounded) on per-supernode
                          completion counters; 3: cooperative, one launch per sweep that walks the
                          levels separated by bounded grid-wide barriers; 0: default (1) */
   int rows_per_lane_fwd; /* rows per lane of the forward sweep alone (0: rows_per_lane if set,
-                            else the forward default: 2 for W >= 256, 1 below) */
+                            else the forward default: 2 for W >= 256 and for W >= 8 on 2^17 faces
+                            or more, 1 otherwise) */
   int pack_rows;      /* W = 1, level schedule: supernodes of at most this many rows (and at most 8
                          columns) are solved one per lane, 32 per warp (0: default 24; negative:
                          never) ... */

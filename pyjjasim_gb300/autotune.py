@@ -42,7 +42,7 @@ from . import plan as P
 
 CACHE_ENV = "PYJJASIM_GB300_TUNE_CACHE"
 DEFAULT = {"schedule": 1, "ordering": "auto", "relax": (-1, -1.0), "rows_per_lane": 0, "rows_per_lane_fwd": 0,
-           "rhs_block": 0, "target_warps": 152 * 24, "pdl": 0, "groups": 0, "subtree_rows": 0}
+           "rhs_block": 0, "target_warps": 0, "pdl": 0, "groups": 0, "subtree_rows": 0}
 # searched in this order; a tuple is searched jointly (ordering and rows per lane interact:
 # minimum degree's smaller supernodes want fewer rows per warp). Rows per lane 0 = the library's
 # defaults (1, and 2 in the forward sweep from W = 256 on); a nonzero value sets both sweeps
@@ -74,7 +74,7 @@ def candidates(W):
         "rows_per_lane": [0, 1, 2, 4],
         "rows_per_lane_fwd": [0, 1, 2, 4],
         "rhs_block": [0] + [b for b in (wb // 2, wb // 4) if b >= 1],
-        "target_warps": [152 * 24, 152 * 8, 152 * 64],
+        "target_warps": [0, 152 * 8, 152 * 24, 152 * 64],
         "subtree_rows": [0, -1, 24, 48] if W >= 17 else [0, -1, 16, 32],
         "relax": [(-1, -1.0), (0, 0.0), (64, 0.1)],
     }

@@ -80,6 +80,8 @@ constexpr int kGroupsFromW = 256;      // from this many problems the step runs 
 constexpr int kGroupW = 160;           // ... of about this many problems, 2 to 4 of them
 constexpr int kNumSMs = 152;                     // GB300
 constexpr int kDefaultTargetWarps = 152 * 24;   // levels with fewer work items split their dot products
+constexpr int kDefaultTargetWarpsSmallW = 152 * 64;   // ... for 2-16 problems
+constexpr int kFwdWideFaces = 1 << 17;          // forward sweep: two rows per lane from W = 8 on this many faces
 constexpr int kDefaultMinPiece = 16;     // shortest piece of a split dot product
 constexpr int kDefaultSubRows = 32;     // subtree sweeps: rows per subtree (columns + the root's off-diagonal rows)
 constexpr int kSubMaxRows = 64;          // ... at most this many rows (tuning bound)
@@ -1615,11 +1617,23 @@ T* upload(const T* h, size_t n, int64_t& bytes) {
 // rows_per_lane, which sets both; unset fields take each sweep's default. Measured on GB300
 // (ms/step, forward/backward rows): W = 512: 1/1 1.554, 2/1 1.511, 2/2 1.579; W = 1: 1/1 0.133,
 // 2/1 0.138; 64x64 x 64: 1/1 0.138, 2/1 0.141; so two forward rows from W = 256 on.
-int rows_per_lane_of(const jja_solve_tuning& tu, bool forward, int W) {
+// rows per lane of a sweep's work items for W problems on n faces (the forward sweep takes two
+// from W = 256 on, and from W = 8 on arrays of 2^17 faces or more; measured on GB300:
+// SquareArray(512,512) x 8 0.679 -> 0.663 ms, (1024,1024) x 8 2.43 -> 2.32 ms per step,
+// (256,256) x 8 0.252 -> 0.267 ms)
+int rows_per_lane_of(const jja_solve_tuning& tu, bool forward, int W, int n) {
   if (forward && tu.rows_per_lane_fwd) return tu.rows_per_lane_fwd;
   if (tu.rows_per_lane) return tu.rows_per_lane;
-  if (forward) return W >= 256 ? kDefaultRowsPerLaneFwdWide : kDefaultRowsPerLane;
+  if (forward && (W >= 256 || (W >= 8 && n >= kFwdWideFaces))) return kDefaultRowsPerLaneFwdWide;
   return kDefaultRowsPerLane;
+}
+
+// dot products of levels with fewer work items than this are split (split target): wider for
+// 2-16 problems (measured on GB300: SquareArray(1024,1024) x 8 2.56 -> 2.43 ms per step,
+// (512,512) x 8 0.699 -> 0.679; unchanged at W = 1 and W = 512 on 128x128 and 512x512)
+int target_warps_of(const jja_solve_tuning& tu, int W) {
+  if (tu.target_warps) return tu.target_warps;
+  return (W >= 2 && W <= 16) ? kDefaultTargetWarpsSmallW : kDefaultTargetWarps;
 }
 
 // problems per warp of the triangular solves
@@ -1875,10 +1889,10 @@ Schedule build_schedule(const jja::Factor& F, int W, const jja_solve_tuning& tu,
                             ? (tu.pack_rows ? tu.pack_rows : kDefaultPackRows) : 0;
 
   const int64_t pack_min_warps = tu.pack_min_warps ? tu.pack_min_warps : kDefaultPackMinWarps;
-  const int target_warps = tu.target_warps ? tu.target_warps : kDefaultTargetWarps;
+  const int target_warps = target_warps_of(tu, W);
   const int min_piece = tu.min_piece ? tu.min_piece : kDefaultMinPiece;
   const int LG = 32 / WB;
-  const int RPI_f = LG * rows_per_lane_of(tu, true, W), RPI_b = LG * rows_per_lane_of(tu, false, W);
+  const int RPI_f = LG * rows_per_lane_of(tu, true, W, F.n), RPI_b = LG * rows_per_lane_of(tu, false, W, F.n);
   Schedule S;
   S.n_levels = F.n_levels;
   S.ns = F.ns;
@@ -2755,8 +2769,8 @@ int jja_plan_create(const jja_plan_desc* d, const jja_factor* fac, jja_plan** ou
     // by build_schedule
     const jja_solve_tuning& tu = d->tuning;
     p->WB = resolve_rhs_block(d->W, tu);
-    p->rows_per_lane = rows_per_lane_of(tu, false, d->W);
-    p->rows_per_lane_fwd = rows_per_lane_of(tu, true, d->W);
+    p->rows_per_lane = rows_per_lane_of(tu, false, d->W, F.n);
+    p->rows_per_lane_fwd = rows_per_lane_of(tu, true, d->W, F.n);
     p->pdl = tu.pdl == 1;
     p->dst_lines = tu.dst_lines;
     const int Nj = d->Nj, Nf = d->Nf;
