@@ -189,3 +189,20 @@ def test_ctypes_structs_match_the_header():
                             ("jja_adjoint_segment_args", N.AdjointSegmentArgs), ("jja_factor_opts", N.FactorOpts),
                             ("jja_factor_stats", N.FactorStats), ("jja_schedule_stats", N.ScheduleStats)):
         assert c_fields(cname) == [f for f, _ in pystruct._fields_], cname
+
+
+def test_default_launch_shape_rules():
+    """The library's defaults equal the explicit settings they stand for: two forward rows per
+    lane from W = 8 on arrays of 2^17 faces or more (and from W = 256 everywhere), one below; a
+    split target of 152 x 64 warps for 2-16 problems, 152 x 24 otherwise."""
+    def sched(n, W, tuning):
+        f = P.get_factor(SquareArray(n, n), 0.05, nd_leaf=8, ordering="nd")[0]
+        st = f.schedule_stats(W, dict(tuning, subtree_rows=-1))
+        return st["n_fwd_items"], st["n_bwd_items"]
+
+    big, small = 400, 256                  # 159 201 and 65 025 faces
+    assert sched(big, 8, {}) == sched(big, 8, {"rows_per_lane_fwd": 2, "target_warps": 152 * 64})
+    assert sched(big, 8, {}) != sched(big, 8, {"rows_per_lane_fwd": 1, "target_warps": 152 * 64})
+    assert sched(small, 8, {}) == sched(small, 8, {"rows_per_lane_fwd": 1, "target_warps": 152 * 64})
+    assert sched(small, 1, {}) == sched(small, 1, {"rows_per_lane_fwd": 1, "target_warps": 152 * 24})
+    assert sched(small, 512, {}) == sched(small, 512, {"rows_per_lane_fwd": 2, "target_warps": 152 * 24})
